@@ -1,0 +1,188 @@
+/*
+ * wakis_fit.h -- C ABI of the GB300 (sm_103a) Finite Integration Technique leapfrog path.
+ *
+ * One context (FitCtx) holds one rectilinear grid: the caller-owned field storage
+ * E, H, J (device pointers, 3*N elements each, component blocks [x | y | z], each block
+ * in Fortran order n = i + Nx*j + Nx*Ny*k), the library-owned per-edge / per-face
+ * coefficient arrays, the optional fused sources (beam line current, hard plane
+ * source), the optional wake-potential line taps and the step machinery.
+ *
+ * Every entry point returns 0 (FIT_OK) or a negative FIT_ERR_* code; the message of
+ * the last failure is available through fit_last_error().  Device faults are never
+ * turned into traps: kernels write error codes that the host reads.
+ *
+ * Pointers documented as "device" must be CUDA device pointers on the context's
+ * device; "host" pointers are plain host memory read during the call.
+ * Citations name the reference interface (Wakis 0.7.0) each entry point replaces.
+ */
+#ifndef WAKIS_FIT_H
+#define WAKIS_FIT_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define FIT_API __attribute__((visibility("default")))
+#else
+#define FIT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIT_OK 0
+#define FIT_ERR_ARG (-1)
+#define FIT_ERR_CUDA (-2)
+#define FIT_ERR_STATE (-3)
+#define FIT_ERR_TIMEOUT (-4)
+#define FIT_ERR_NOMEM (-5)
+#define FIT_ERR_DEVICE (-6)
+
+#define FIT_F32 0
+#define FIT_F64 1
+
+/* boundary codes per face (wakis/boundaries.py:14-188) */
+#define FIT_BC_PERIODIC 0
+#define FIT_BC_PEC 1 /* 'pec' or 'electric' */
+#define FIT_BC_PML 2
+#define FIT_BC_PMC 3 /* 'pmc' or 'magnetic' */
+#define FIT_BC_ABC 4
+
+/* E-pass variants: how the conduction current J enters the E update
+ * (wakis/solverFIT3D.py:514-525). */
+#define FIT_J_ELIDED 0   /* J == sigma*E of the previous step (or 0): folded into a loss factor */
+#define FIT_J_EXPLICIT 1 /* J read from storage; J = sigma*E written back when conductive */
+#define FIT_STEP_NO_BEAM 2 /* or-ed into j_mode: the beam line current is off for this step */
+
+typedef struct FitCtx FitCtx;
+
+typedef struct FitGridDesc {
+    int64_t nx, ny, nz;
+    int32_t dtype;            /* FIT_F32 or FIT_F64: storage and stencil arithmetic */
+    int32_t use_conductivity; /* SolverFIT3D.use_conductivity */
+    int32_t bc_lo[3];         /* FIT_BC_* for the x, y, z low faces */
+    int32_t bc_hi[3];         /* FIT_BC_* for the x, y, z high faces */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t reserved;
+    void *E, *H, *J; /* device, 3*N elements of dtype each (caller-owned) */
+} FitGridDesc;
+
+/* Context lifetime.  Replaces the operator assembly of SolverFIT3D.__init__
+ * (wakis/solverFIT3D.py:203-227, 337-344): no sparse matrix is built. */
+FIT_API int fit_ctx_create(const FitGridDesc *desc, FitCtx **out);
+FIT_API int fit_ctx_destroy(FitCtx *ctx);
+/* Copies the last error message (NUL terminated, truncated to len); ctx may be NULL
+ * for errors raised by fit_ctx_create. */
+FIT_API int fit_last_error(const FitCtx *ctx, char *buf, int64_t len);
+/* Stream (cudaStream_t) every later launch of this context is issued on; NULL = legacy. */
+FIT_API int fit_set_stream(FitCtx *ctx, void *stream);
+/* Rebinds E, H, J (device) after the caller reallocated them. */
+FIT_API int fit_set_fields(FitCtx *ctx, void *E, void *H, void *J);
+
+/* Grid metrics (wakis/gridFIT3D.py:263-305): host FP64 arrays of primal edge lengths
+ * dx[nx], dy[ny], dz[nz] and UNEDITED dual edge lengths tdx[nx], tdy[ny], tdz[nz]
+ * (last entry 0).  Periodic / ABC edits of tL and itA (wakis/boundaries.py:36-70,
+ * 153-181) are applied by the library from the face codes. */
+FIT_API int fit_set_metrics(FitCtx *ctx, const double *dx, const double *dy, const double *dz,
+                    const double *tdx, const double *tdy, const double *tdz);
+
+/* Coefficients from FP64 material tensors (device, 3*N each): ieps = 1/eps, imu = 1/mu,
+ * sigma.  Builds, on the device in FP64 and stores in the field dtype,
+ *   ch = dt*iA*imu*[PMC row mask]          (H pass, the tDs.iDmu.iDa.C operator)
+ *   ce = dt*ieps*itA*[PEC row mask]        (E pass, the itDa.iDeps.C^T.tDs operator)
+ *   cl = 1 - dt*ieps*sigma                 (loss factor of the elided-J E pass)
+ * (wakis/solverFIT3D.py:337-344, 378-436).  The material arrays are read during the call
+ * only, except that FIT_J_EXPLICIT steps keep a dtype copy of dt*ieps and sigma. */
+FIT_API int fit_set_coeffs(FitCtx *ctx, double dt, const double *ieps, const double *imu,
+                   const double *sigma);
+/* Allocates the dtype copies of dt*ieps and sigma that FIT_J_EXPLICIT steps read
+ * (J set by the caller, wakis/solverFIT3D.py:514-525); the next fit_set_coeffs fills them. */
+FIT_API int fit_enable_explicit_j(FitCtx *ctx);
+
+/* Zeroes the ghost tangential components on the last index planes, as the first
+ * one_step does (wakis/solverFIT3D.py:505-508, 842-862). */
+FIT_API int fit_zero_ghosts(FitCtx *ctx);
+
+/* Gaussian beam line current J_z(ixs, iys, :) of sources.Beam.update
+ * (wakis/sources.py:76-110), evaluated inside the E pass:
+ *   J_z(k) = q*v*[exp(-((z_k - vt) - s0)^2 / (2 sigmaz^2)) / sqrt(2 pi sigmaz^2)] / dx / dy
+ * z (host, nz cell-centre coordinates), ieps_line (host, nz values of ieps_z on the line).
+ * active = 0 removes the beam. */
+FIT_API int fit_set_beam(FitCtx *ctx, int32_t active, int32_t ixs, int32_t iys, double q, double v,
+                 double sigmaz, double s0, double dx_s, double dy_s, const double *z,
+                 const double *ieps_line);
+/* Per-step beam position v*t.  Either one value for the next host-driven step, or a
+ * table (host, n entries) indexed by the step number for fit_run. */
+FIT_API int fit_set_beam_vt(FitCtx *ctx, double vt);
+FIT_API int fit_set_beam_vt_table(FitCtx *ctx, const double *vt, int64_t n);
+
+/* Hard plane source of sources.PlaneWave / sources.WavePacket (wakis/sources.py:218-248,
+ * 373-420): at step n, before the H pass,
+ *   H_y(i, j, zs) = (c1[n] * g[i-x0, j-y0]) * gt[n]  and  E_x(i, j, zs) = (c2[n] * g) * gt[n]
+ * for x0 <= i < x1, y0 <= j < y1.  prof (host, (x1-x0)*(y1-y0) values, x fastest) may be
+ * NULL for g = 1.  c1, c2, gt (host, n entries each).  active = 0 removes it. */
+FIT_API int fit_set_plane_source(FitCtx *ctx, int32_t active, int32_t zs, int32_t x0, int32_t x1,
+                         int32_t y0, int32_t y1, const double *prof, const double *c1,
+                         const double *c2, const double *gt, int64_t n);
+
+/* First-order ABC of emsolve on the CPU reference (wakis/routines.py:183-220,
+ * wakis/boundaries.py:307-404): after each step the index-1 plane of E and H is copied
+ * to the index-0 plane for every axis bit set in lo_axes (bit 0 = x, 1 = y, 2 = z). */
+FIT_API int fit_set_abc(FitCtx *ctx, int32_t lo_axes);
+
+/* Wake-potential line taps (wakis/wakeSolver.py:423-551).  nlines transverse lines at
+ * cells (lx[l], ly[l]) (host); a tap table in CSR over steps (host): entries of step n
+ * are row_ptr[n] .. row_ptr[n+1]-1, each adding
+ *   sum_{c < cnt} E_z(lx, ly, k0 + c + kskip) * dz[k0 + c]
+ * to accumulator (line, m) with FP64 Neumaier compensation.  dz (host, nz_tap values).
+ * Replaces the per-step Ez.h5 dump (wakis/routines.py:422-445) and the interpreted
+ * integral loop. */
+FIT_API int fit_set_wake_taps(FitCtx *ctx, int32_t nlines, const int32_t *lx, const int32_t *ly,
+                      int32_t kskip, int32_t ns, int64_t nsteps, const int64_t *row_ptr,
+                      const int32_t *ent_m, const int32_t *ent_k0, const int32_t *ent_cnt,
+                      int32_t nz_tap, const double *dz);
+FIT_API int fit_reset_wake(FitCtx *ctx);
+/* Raw line integrals (host out, nlines*ns FP64, line-major). */
+FIT_API int fit_read_wake(FitCtx *ctx, double *out);
+
+/* One leapfrog step (wakis/solverFIT3D.py:504-525) at step number n with the given
+ * J variant (FIT_J_*, optionally | FIT_STEP_NO_BEAM):
+ * [plane source, wake taps at E^n] -> H pass -> E pass (+beam) -> [ABC]. */
+FIT_API int fit_step(FitCtx *ctx, int64_t n, int32_t j_mode);
+/* nsteps steps n0 .. n0+nsteps-1 with the elided-J E pass, the beam vt taken from the
+ * vt table and the step number read on the device (CUDA-graph replay of chunks). */
+FIT_API int fit_run(FitCtx *ctx, int64_t n0, int64_t nsteps);
+
+/* Brings the J storage up to date (the J of wakis/solverFIT3D.py:524-525 and
+ * wakis/sources.py:108-110): flags bit 0 writes J = sigma*E in the field dtype from FP64
+ * sigma (device, 3*N; conductive contexts only), bit 1 then writes the beam line current
+ * at the vt of fit_set_beam_vt. */
+FIT_API int fit_materialize_J(FitCtx *ctx, const double *sigma, int32_t flags);
+
+/* Wake post-processing on the device in FP64 (wakis/wakeSolver.py:480-611):
+ * raw (device-resident accumulators of fit_set_wake_taps) combined line by line as
+ * WP_3d[l] = (WP_3d[l-1] + raw[l]) / qscale, then the Panofsky-Wenzel transverse
+ * wake from exclusive prefix sums along s (ds) and the central differences over
+ * dxf = (dxf0 + dxf1), dyf = (dyf0 + dyf1).  Outputs (host): wp3d (nlines*ns),
+ * wpx, wpy (ns each; untouched when nlines != 9). */
+FIT_API int fit_wake_finalize(FitCtx *ctx, double qscale, double ds, double dxf, double dyf,
+                      double *wp3d, double *wpx, double *wpy);
+
+/* FP64 direct DFT at bins b0 .. b0+nb-1 of an n-point zero-padded transform
+ *   X_s[b] = sum_{t < len} x_s[t] exp(-2 pi i b t / n)
+ * for nsig signals of length len (host, signal-major); out (host) holds nsig*nb
+ * (re, im) pairs.  Replaces np.fft.fft(..., n=N)[mask] (wakis/wakeSolver.py:692-699,
+ * 755-770).  Uses library-allocated device scratch for partial sums. */
+FIT_API int fit_dft(const double *x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
+            double *out);
+
+/* Library build information: sm architecture compiled for, and the kernel launch
+ * counter (kernels issued since load), for bench accounting. */
+FIT_API int fit_version(char *buf, int64_t len);
+FIT_API int64_t fit_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WAKIS_FIT_H */

@@ -1,0 +1,859 @@
+// fit_capi.cu -- extern "C" entry points of libwakis_fit.so (declared in include/wakis_fit.h).
+//
+// A context owns: the coefficient arrays in the field dtype, the 1-D metric arrays, the
+// source / tap tables, a private non-blocking stream on which every kernel is issued
+// (ordered after and before the caller's stream with events, so caller writes to the
+// fields and our kernels never race), and the CUDA graphs of fit_run.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "wakis_fit.h"
+#include "fit_kernels.cuh"
+
+using namespace fit;
+
+namespace {
+
+std::atomic<long long> g_launches{0};
+std::mutex g_err_mu;
+std::string g_create_error;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct FitCtx {
+    int device = 0;
+    int dtype = FIT_F32;
+    int use_cond = 0;
+    Geom g{};
+    int bc_lo[3]{}, bc_hi[3]{};
+    int edits[6]{};
+    int n_edits = 0;
+    void *E = nullptr, *H = nullptr, *J = nullptr;
+    cudaStream_t user = nullptr;  // caller stream (may be the legacy default stream)
+    cudaStream_t own = nullptr;   // private stream all kernels run on
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    // metrics: FP64 (coefficient build) and field-dtype copies (stencil)
+    double* dL[3]{};
+    double* dtL0[3]{};  // unedited dual lengths
+    void* tL_T[3]{};
+    void* L_T[3]{};
+    bool metrics_set = false;
+    // coefficients
+    void *ch = nullptr, *ce = nullptr, *cl = nullptr, *cj = nullptr, *sg = nullptr;
+    bool coeffs_set = false;
+    bool explicit_ready = false;
+    double dt = 0.0;
+    // beam
+    BeamArgs beam{};
+    double* d_beam_z = nullptr;
+    double* d_beam_dtieps = nullptr;
+    std::vector<double> ieps_line;
+    double beam_vt = 0.0;
+    double* d_vt_table = nullptr;
+    long long vt_len = 0;
+    // plane source
+    PlaneArgs plane{};
+    double *d_prof = nullptr, *d_c1 = nullptr, *d_c2 = nullptr, *d_gt = nullptr, *d_stash = nullptr;
+    // abc
+    int abc_axes = 0;
+    // wake taps
+    TapArgs tap{};
+    long long *d_base = nullptr, *d_row = nullptr;
+    int *d_em = nullptr, *d_ek0 = nullptr, *d_ecnt = nullptr;
+    double *d_dz = nullptr, *d_acc = nullptr, *d_comp = nullptr, *d_scratch = nullptr;
+    double *d_wp3d = nullptr, *d_wpx = nullptr, *d_wpy = nullptr;
+    // step counter and graphs
+    long long* d_step = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    long long graph_chunk = 0;
+    bool capturing = false;
+    std::string err;
+};
+
+namespace {
+
+int fail(FitCtx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) {
+        c->err = buf;
+    } else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        g_create_error = buf;
+    }
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(c, FIT_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));     \
+    } while (0)
+
+size_t esize(const FitCtx* c) { return c->dtype == FIT_F64 ? 8 : 4; }
+
+int dev_alloc(FitCtx* c, void** p, size_t bytes) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (bytes == 0) return FIT_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(c, e == cudaErrorMemoryAllocation ? FIT_ERR_NOMEM : FIT_ERR_CUDA,
+                    "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    return FIT_OK;
+}
+
+template <typename P>
+int upload(FitCtx* c, P** dst, const void* src, size_t bytes) {
+    int rc = dev_alloc(c, reinterpret_cast<void**>(dst), bytes);
+    if (rc) return rc;
+    if (bytes) CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, c->own));
+    return FIT_OK;
+}
+
+void dfree(void* p) {
+    if (p) cudaFree(p);
+}
+
+// ordering with the caller's stream
+int enter(FitCtx* c) {
+    CK(cudaSetDevice(c->device));
+    CK(cudaEventRecord(c->ev_in, c->user));
+    CK(cudaStreamWaitEvent(c->own, c->ev_in, 0));
+    return FIT_OK;
+}
+int leave(FitCtx* c) {
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev_out, c->own));
+    CK(cudaStreamWaitEvent(c->user, c->ev_out, 0));
+    return FIT_OK;
+}
+
+int pick_vec(const FitCtx* c) {
+    const int nx = c->g.nx;
+    if (c->dtype == FIT_F32) return (nx % 4 == 0) ? 4 : (nx % 2 == 0 ? 2 : 1);
+    return (nx % 2 == 0) ? 2 : 1;
+}
+
+template <typename T>
+Metric<T> metric(const FitCtx* c) {
+    Metric<T> m;
+    for (int a = 0; a < 3; ++a) {
+        m.L[a] = static_cast<const T*>(c->L_T[a]);
+        m.tL[a] = static_cast<const T*>(c->tL_T[a]);
+    }
+    return m;
+}
+
+unsigned grid1d(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void count(const FitCtx* c, long long k = 1) {
+    if (!c->capturing) g_launches += k;
+}
+
+// any change of what a captured step launches drops the graph
+void invalidate(FitCtx* c) {
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+}
+
+int launches_per_step(const FitCtx* c) {
+    int n = 3;
+    for (int a = 0; a < 3; ++a) n += (c->abc_axes >> a) & 1;
+    return n;
+}
+
+template <typename T, int VEC>
+void launch_h(FitCtx* c) {
+    const long long nv = c->g.N / VEC;
+    k_hpass<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
+                                                         static_cast<const T*>(c->ch), c->g, metric<T>(c));
+    count(c);
+}
+
+template <typename T, int VEC>
+void launch_e(FitCtx* c, int mode, const StepArgs& st) {
+    const long long nv = c->g.N / VEC;
+    const unsigned nb = grid1d(nv, 256);
+    T* E = static_cast<T*>(c->E);
+    const T* H = static_cast<const T*>(c->H);
+    const T* ce = static_cast<const T*>(c->ce);
+    const T* cl = static_cast<const T*>(c->cl);
+    T* J = static_cast<T*>(c->J);
+    const T* cj = static_cast<const T*>(c->cj);
+    const T* sg = static_cast<const T*>(c->sg);
+    if (mode == 0)
+        k_epass<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
+    else if (mode == 1)
+        k_epass<T, VEC, 1><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
+    else
+        k_epass<T, VEC, 2><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
+    count(c);
+}
+
+template <typename T>
+void launch_step_t(FitCtx* c, long long n, int mode, bool device_step) {
+    StepArgs st{};
+    if (device_step) {
+        st.d_step = c->d_step;
+        st.vt_table = c->d_vt_table;
+        st.vt_len = c->vt_len;
+    } else {
+        st.n = n;
+        st.vt = c->beam_vt;
+    }
+    const bool need_pro = device_step || c->plane.active || c->tap.nlines > 0;
+    if (need_pro) {
+        k_prologue<T><<<1, 512, 0, c->own>>>(static_cast<T*>(c->E), static_cast<T*>(c->H), c->g, c->plane, c->tap,
+                                             n, device_step ? c->d_step : nullptr);
+        count(c);
+    }
+    const int vec = pick_vec(c);
+    if (vec == 4) {
+        if constexpr (sizeof(T) == 4) {
+            launch_h<T, 4>(c);
+            launch_e<T, 4>(c, mode, st);
+        }
+    } else if (vec == 2) {
+        launch_h<T, 2>(c);
+        launch_e<T, 2>(c, mode, st);
+    } else {
+        launch_h<T, 1>(c);
+        launch_e<T, 1>(c, mode, st);
+    }
+    for (int a = 0; a < 3; ++a) {
+        if (c->abc_axes & (1 << a)) {
+            const int pa = a == 0 ? c->g.ny : c->g.nx;
+            const int pb = a == 2 ? c->g.ny : c->g.nz;
+            k_abc_lo<T><<<grid1d(6LL * pa * pb, 256), 256, 0, c->own>>>(static_cast<T*>(c->E), static_cast<T*>(c->H),
+                                                                     c->g, a);
+            count(c);
+        }
+    }
+}
+
+void launch_step(FitCtx* c, long long n, int mode, bool device_step) {
+    if (c->dtype == FIT_F64)
+        launch_step_t<double>(c, n, mode, device_step);
+    else
+        launch_step_t<float>(c, n, mode, device_step);
+}
+
+int check_ready(FitCtx* c) {
+    if (!c) return FIT_ERR_ARG;
+    if (!c->metrics_set) return fail(c, FIT_ERR_STATE, "fit_set_metrics has not been called");
+    if (!c->coeffs_set) return fail(c, FIT_ERR_STATE, "fit_set_coeffs has not been called");
+    if (!c->E || !c->H || !c->J) return fail(c, FIT_ERR_STATE, "field pointers are not set");
+    return FIT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
+    FitCtx* c = nullptr;
+    if (!d || !out) return fail(nullptr, FIT_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (d->nx < 1 || d->ny < 1 || d->nz < 1)
+        return fail(nullptr, FIT_ERR_ARG, "grid dimensions must be >= 1 (got %lld x %lld x %lld)",
+                    (long long)d->nx, (long long)d->ny, (long long)d->nz);
+    const long long N = d->nx * d->ny * d->nz;
+    if (3 * N >= (1LL << 31) * 2LL)
+        return fail(nullptr, FIT_ERR_ARG, "grid too large: 3*N = %lld", 3 * N);
+    if (d->dtype != FIT_F32 && d->dtype != FIT_F64) return fail(nullptr, FIT_ERR_ARG, "dtype must be FIT_F32 or FIT_F64");
+    for (int a = 0; a < 3; ++a)
+        if (d->bc_lo[a] < 0 || d->bc_lo[a] > 4 || d->bc_hi[a] < 0 || d->bc_hi[a] > 4)
+            return fail(nullptr, FIT_ERR_ARG, "invalid boundary code on axis %d", a);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, FIT_ERR_DEVICE, "no CUDA device available");
+    if (d->device < 0 || d->device >= ndev) return fail(nullptr, FIT_ERR_ARG, "invalid device %d", d->device);
+    c = new FitCtx();
+    c->device = d->device;
+    c->dtype = d->dtype;
+    c->use_cond = d->use_conductivity ? 1 : 0;
+    c->g.nx = (int)d->nx;
+    c->g.ny = (int)d->ny;
+    c->g.nz = (int)d->nz;
+    c->g.N = N;
+    c->g.sy = d->nx;
+    c->g.sz = d->nx * d->ny;
+    // face masks (wakis/boundaries.py:73-150)
+    unsigned pec = 0, pmc = 0;
+    bool any_pmc = false;
+    for (int a = 0; a < 3; ++a) {
+        c->bc_lo[a] = d->bc_lo[a];
+        c->bc_hi[a] = d->bc_hi[a];
+        if (d->bc_lo[a] == FIT_BC_PEC || d->bc_lo[a] == FIT_BC_PML) pec |= 1u << (2 * a);
+        if (d->bc_hi[a] == FIT_BC_PEC || d->bc_hi[a] == FIT_BC_PML) pec |= 1u << (2 * a + 1);
+        if (d->bc_lo[a] == FIT_BC_PMC) { pmc |= 1u << (2 * a); any_pmc = true; }
+        if (d->bc_hi[a] == FIT_BC_PMC) { pmc |= 1u << (2 * a + 1); any_pmc = true; }
+    }
+    c->g.pec = pec;
+    c->g.pmc = any_pmc ? (pmc | pec) : 0u;  // the PMC mask starts from the PEC face values
+    // periodic edits (x, y, z) then ABC high-face edits (x, y, z)
+    bool any_periodic_lo = false;
+    for (int a = 0; a < 3; ++a) any_periodic_lo |= d->bc_lo[a] == FIT_BC_PERIODIC;
+    if (any_periodic_lo)
+        for (int a = 0; a < 3; ++a)
+            if (d->bc_lo[a] == FIT_BC_PERIODIC && d->bc_hi[a] == FIT_BC_PERIODIC) c->edits[c->n_edits++] = a;
+    bool any_abc = false;
+    for (int a = 0; a < 3; ++a) any_abc |= d->bc_lo[a] == FIT_BC_ABC || d->bc_hi[a] == FIT_BC_ABC;
+    if (any_abc)
+        for (int a = 0; a < 3; ++a)
+            if (d->bc_hi[a] == FIT_BC_ABC) c->edits[c->n_edits++] = a;
+    c->E = d->E;
+    c->H = d->H;
+    c->J = d->J;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_step, sizeof(long long));
+    if (e != cudaSuccess) {
+        int rc = fail(nullptr, FIT_ERR_CUDA, "context setup failed: %s", cudaGetErrorString(e));
+        fit_ctx_destroy(c);
+        return rc;
+    }
+    const size_t fb = 3 * (size_t)N * esize(c);
+    int rc = dev_alloc(c, &c->ch, fb);
+    if (!rc) rc = dev_alloc(c, &c->ce, fb);
+    if (!rc && c->use_cond) rc = dev_alloc(c, &c->cl, fb);
+    if (rc) {
+        std::string m = c->err;
+        fit_ctx_destroy(c);
+        return fail(nullptr, rc, "%s", m.c_str());
+    }
+    *out = c;
+    return FIT_OK;
+}
+
+int fit_ctx_destroy(FitCtx* c) {
+    if (!c) return FIT_OK;
+    cudaSetDevice(c->device);
+    if (c->own) cudaStreamSynchronize(c->own);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (int a = 0; a < 3; ++a) {
+        dfree(c->dL[a]);
+        dfree(c->dtL0[a]);
+        dfree(c->tL_T[a]);
+        dfree(c->L_T[a]);
+    }
+    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg}) dfree(p);
+    for (void* p : {(void*)c->d_beam_z, (void*)c->d_beam_dtieps, (void*)c->d_vt_table, (void*)c->d_prof,
+                    (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
+                    (void*)c->d_em, (void*)c->d_ek0, (void*)c->d_ecnt, (void*)c->d_dz, (void*)c->d_acc,
+                    (void*)c->d_comp, (void*)c->d_scratch, (void*)c->d_wp3d, (void*)c->d_wpx, (void*)c->d_wpy,
+                    (void*)c->d_step})
+        dfree(p);
+    if (c->ev_in) cudaEventDestroy(c->ev_in);
+    if (c->ev_out) cudaEventDestroy(c->ev_out);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return FIT_OK;
+}
+
+int fit_last_error(const FitCtx* c, char* buf, int64_t len) {
+    if (!buf || len <= 0) return FIT_ERR_ARG;
+    std::string m;
+    if (c) {
+        m = c->err;
+    } else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        m = g_create_error;
+    }
+    snprintf(buf, (size_t)len, "%s", m.c_str());
+    return FIT_OK;
+}
+
+int fit_set_stream(FitCtx* c, void* stream) {
+    if (!c) return FIT_ERR_ARG;
+    c->user = static_cast<cudaStream_t>(stream);
+    return FIT_OK;
+}
+
+int fit_set_fields(FitCtx* c, void* E, void* H, void* J) {
+    if (!c || !E || !H || !J) return fail(c, FIT_ERR_ARG, "null field pointer");
+    invalidate(c);
+    c->E = E;
+    c->H = H;
+    c->J = J;
+    return FIT_OK;
+}
+
+int fit_set_metrics(FitCtx* c, const double* dx, const double* dy, const double* dz, const double* tdx,
+                    const double* tdy, const double* tdz) {
+    if (!c || !dx || !dy || !dz || !tdx || !tdy || !tdz) return fail(c, FIT_ERR_ARG, "null metric array");
+    invalidate(c);
+    int rc = enter(c);
+    if (rc) return rc;
+    const double* L[3] = {dx, dy, dz};
+    const double* T0[3] = {tdx, tdy, tdz};
+    const int len[3] = {c->g.nx, c->g.ny, c->g.nz};
+    bool edited[3] = {false, false, false};
+    for (int e = 0; e < c->n_edits; ++e) edited[c->edits[e]] = true;
+    for (int a = 0; a < 3; ++a) {
+        std::vector<double> tl(T0[a], T0[a] + len[a]);
+        if (edited[a]) tl[len[a] - 1] = L[a][0];  // tL[-1] = L[0] (wakis/boundaries.py:41,157)
+        rc = upload(c, &c->dL[a], L[a], len[a] * sizeof(double));
+        if (!rc) rc = upload(c, &c->dtL0[a], T0[a], len[a] * sizeof(double));
+        if (rc) return rc;
+        if (c->dtype == FIT_F64) {
+            rc = upload(c, reinterpret_cast<double**>(&c->L_T[a]), L[a], len[a] * sizeof(double));
+            if (!rc) rc = upload(c, reinterpret_cast<double**>(&c->tL_T[a]), tl.data(), len[a] * sizeof(double));
+        } else {
+            std::vector<float> lf(L[a], L[a] + len[a]), tf(tl.begin(), tl.end());
+            rc = upload(c, reinterpret_cast<float**>(&c->L_T[a]), lf.data(), len[a] * sizeof(float));
+            if (!rc) rc = upload(c, reinterpret_cast<float**>(&c->tL_T[a]), tf.data(), len[a] * sizeof(float));
+            if (!rc) CK(cudaStreamSynchronize(c->own));  // host vectors die here
+        }
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(c->own));
+    c->metrics_set = true;
+    return leave(c);
+}
+
+int fit_enable_explicit_j(FitCtx* c) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->explicit_ready) return FIT_OK;
+    const size_t fb = 3 * (size_t)c->g.N * esize(c);
+    int rc = dev_alloc(c, &c->cj, fb);
+    if (!rc) rc = dev_alloc(c, &c->sg, fb);
+    if (rc) return rc;
+    invalidate(c);
+    c->explicit_ready = true;
+    c->coeffs_set = false;  // cj / sg must be filled by fit_set_coeffs
+    return FIT_OK;
+}
+
+int fit_set_coeffs(FitCtx* c, double dt, const double* ieps, const double* imu, const double* sigma) {
+    if (!c || !ieps || !imu || !sigma) return fail(c, FIT_ERR_ARG, "null material array");
+    if (!c->metrics_set) return fail(c, FIT_ERR_STATE, "fit_set_metrics must precede fit_set_coeffs");
+    int rc = enter(c);
+    if (rc) return rc;
+    CoeffArgs a{};
+    for (int i = 0; i < 3; ++i) {
+        a.L[i] = c->dL[i];
+        a.tL[i] = c->dtL0[i];
+    }
+    for (int e = 0; e < c->n_edits; ++e) a.edits[e] = c->edits[e];
+    a.n_edits = c->n_edits;
+    a.dt = dt;
+    a.use_cond = c->use_cond;
+    const long long n3 = 3 * c->g.N;
+    if (c->dtype == FIT_F64)
+        k_build_coeffs<double><<<grid1d(n3, 256), 256, 0, c->own>>>(
+            ieps, imu, sigma, (double*)c->ch, (double*)c->ce, (double*)c->cl, (double*)c->cj, (double*)c->sg, c->g, a);
+    else
+        k_build_coeffs<float><<<grid1d(n3, 256), 256, 0, c->own>>>(
+            ieps, imu, sigma, (float*)c->ch, (float*)c->ce, (float*)c->cl, (float*)c->cj, (float*)c->sg, c->g, a);
+    count(c);
+    c->dt = dt;
+    // beam line dt*ieps
+    if (c->beam.active && !c->ieps_line.empty()) {
+        std::vector<double> v(c->ieps_line.size());
+        for (size_t k = 0; k < v.size(); ++k) v[k] = dt * c->ieps_line[k];
+        invalidate(c);
+        rc = upload(c, &c->d_beam_dtieps, v.data(), v.size() * sizeof(double));
+        if (rc) return rc;
+        c->beam.dtieps = c->d_beam_dtieps;
+        CK(cudaStreamSynchronize(c->own));
+    }
+    c->coeffs_set = true;
+    return leave(c);
+}
+
+int fit_zero_ghosts(FitCtx* c) {
+    if (!c || !c->E || !c->H) return fail(c, FIT_ERR_STATE, "fields not set");
+    int rc = enter(c);
+    if (rc) return rc;
+    if (c->dtype == FIT_F64)
+        k_zero_ghosts<double><<<grid1d(c->g.N, 256), 256, 0, c->own>>>((double*)c->E, (double*)c->H, c->g);
+    else
+        k_zero_ghosts<float><<<grid1d(c->g.N, 256), 256, 0, c->own>>>((float*)c->E, (float*)c->H, c->g);
+    g_launches++;
+    return leave(c);
+}
+
+int fit_set_beam(FitCtx* c, int32_t active, int32_t ixs, int32_t iys, double q, double v, double sigmaz, double s0,
+                 double dx_s, double dy_s, const double* z, const double* ieps_line) {
+    if (!c) return FIT_ERR_ARG;
+    invalidate(c);
+    if (!active) {
+        c->beam.active = 0;
+        return FIT_OK;
+    }
+    if (ixs < 0 || ixs >= c->g.nx || iys < 0 || iys >= c->g.ny) return fail(c, FIT_ERR_ARG, "beam cell out of range");
+    if (!z || !ieps_line) return fail(c, FIT_ERR_ARG, "null beam array");
+    if (!(sigmaz > 0)) return fail(c, FIT_ERR_ARG, "sigmaz must be > 0");
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = upload(c, &c->d_beam_z, z, c->g.nz * sizeof(double));
+    if (rc) return rc;
+    c->ieps_line.assign(ieps_line, ieps_line + c->g.nz);
+    std::vector<double> dv(c->g.nz);
+    for (int k = 0; k < c->g.nz; ++k) dv[k] = c->dt * ieps_line[k];
+    rc = upload(c, &c->d_beam_dtieps, dv.data(), dv.size() * sizeof(double));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->own));
+    BeamArgs& b = c->beam;
+    b.active = 1;
+    b.ixs = ixs;
+    b.iys = iys;
+    b.qv = q * v;
+    // numpy evaluates 2 * np.pi * sigmaz**2 as (2*pi)*(sigmaz*sigmaz)
+    const double s2 = sigmaz * sigmaz;
+    b.c0 = 1.0 / sqrt((2.0 * 3.141592653589793) * s2);
+    b.two_s2 = 2.0 * s2;
+    b.s0 = s0;
+    b.dx_s = dx_s;
+    b.dy_s = dy_s;
+    b.z = c->d_beam_z;
+    b.dtieps = c->d_beam_dtieps;
+    return leave(c);
+}
+
+int fit_set_beam_vt(FitCtx* c, double vt) {
+    if (!c) return FIT_ERR_ARG;
+    c->beam_vt = vt;
+    return FIT_OK;
+}
+
+int fit_set_beam_vt_table(FitCtx* c, const double* vt, int64_t n) {
+    if (!c || (!vt && n > 0) || n < 0) return fail(c, FIT_ERR_ARG, "bad vt table");
+    int rc = enter(c);
+    if (rc) return rc;
+    invalidate(c);
+    rc = upload(c, &c->d_vt_table, vt, n * sizeof(double));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->own));
+    c->vt_len = n;
+    return leave(c);
+}
+
+int fit_set_plane_source(FitCtx* c, int32_t active, int32_t zs, int32_t x0, int32_t x1, int32_t y0, int32_t y1,
+                         const double* prof, const double* c1, const double* c2, const double* gt, int64_t n) {
+    if (!c) return FIT_ERR_ARG;
+    invalidate(c);
+    if (!active) {
+        c->plane.active = 0;
+        return FIT_OK;
+    }
+    if (zs < 0 || zs >= c->g.nz || x0 < 0 || x1 > c->g.nx || x0 >= x1 || y0 < 0 || y1 > c->g.ny || y0 >= y1)
+        return fail(c, FIT_ERR_ARG, "plane source region out of range");
+    if (!c1 || !c2 || !gt || n <= 0) return fail(c, FIT_ERR_ARG, "bad plane source tables");
+    int rc = enter(c);
+    if (rc) return rc;
+    const size_t np = (size_t)(x1 - x0) * (y1 - y0);
+    if (prof) {
+        rc = upload(c, &c->d_prof, prof, np * sizeof(double));
+    } else {
+        dfree(c->d_prof);
+        c->d_prof = nullptr;
+    }
+    if (!rc) rc = upload(c, &c->d_c1, c1, n * sizeof(double));
+    if (!rc) rc = upload(c, &c->d_c2, c2, n * sizeof(double));
+    if (!rc) rc = upload(c, &c->d_gt, gt, n * sizeof(double));
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_stash, np * sizeof(double));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->own));
+    PlaneArgs& p = c->plane;
+    p.stash = c->d_stash;
+    p.active = 1;
+    p.zs = zs;
+    p.x0 = x0;
+    p.x1 = x1;
+    p.y0 = y0;
+    p.y1 = y1;
+    p.prof = c->d_prof;
+    p.c1 = c->d_c1;
+    p.c2 = c->d_c2;
+    p.gt = c->d_gt;
+    p.len = n;
+    return leave(c);
+}
+
+int fit_set_abc(FitCtx* c, int32_t lo_axes) {
+    if (!c || lo_axes < 0 || lo_axes > 7) return fail(c, FIT_ERR_ARG, "bad abc axes");
+    const int len[3] = {c->g.nx, c->g.ny, c->g.nz};
+    for (int a = 0; a < 3; ++a)
+        if ((lo_axes >> a) & 1)
+            if (len[a] < 2) return fail(c, FIT_ERR_ARG, "ABC on axis %d needs at least 2 cells", a);
+    if (lo_axes != c->abc_axes) invalidate(c);
+    c->abc_axes = lo_axes;
+    return FIT_OK;
+}
+
+int fit_set_wake_taps(FitCtx* c, int32_t nlines, const int32_t* lx, const int32_t* ly, int32_t kskip, int32_t ns,
+                      int64_t nsteps, const int64_t* row_ptr, const int32_t* ent_m, const int32_t* ent_k0,
+                      const int32_t* ent_cnt, int32_t nz_tap, const double* dz) {
+    if (!c) return FIT_ERR_ARG;
+    invalidate(c);
+    if (nlines <= 0) {
+        c->tap.nlines = 0;
+        return FIT_OK;
+    }
+    if (!lx || !ly || !row_ptr || ns <= 0 || nsteps <= 0 || nz_tap <= 0 || !dz)
+        return fail(c, FIT_ERR_ARG, "bad wake tap arguments");
+    const long long ne = row_ptr[nsteps];
+    if (ne > 0 && (!ent_m || !ent_k0 || !ent_cnt)) return fail(c, FIT_ERR_ARG, "null tap entries");
+    std::vector<long long> base(nlines);
+    for (int l = 0; l < nlines; ++l) {
+        if (lx[l] < 0 || lx[l] >= c->g.nx || ly[l] < 0 || ly[l] >= c->g.ny)
+            return fail(c, FIT_ERR_ARG, "tap line %d outside the grid", l);
+        base[l] = lx[l] + c->g.sy * ly[l] + c->g.sz * (long long)kskip;
+    }
+    for (long long e = 0; e < ne; ++e) {
+        if (ent_m[e] < 0 || ent_m[e] >= ns || ent_k0[e] < 0 || ent_cnt[e] < 1 || ent_k0[e] + ent_cnt[e] > nz_tap ||
+            kskip + ent_k0[e] + ent_cnt[e] > c->g.nz)
+            return fail(c, FIT_ERR_ARG, "tap entry %lld out of range", e);
+    }
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = upload(c, &c->d_base, base.data(), nlines * sizeof(long long));
+    if (!rc) rc = upload(c, &c->d_row, row_ptr, (nsteps + 1) * sizeof(long long));
+    if (!rc) rc = upload(c, &c->d_em, ent_m, ne * sizeof(int));
+    if (!rc) rc = upload(c, &c->d_ek0, ent_k0, ne * sizeof(int));
+    if (!rc) rc = upload(c, &c->d_ecnt, ent_cnt, ne * sizeof(int));
+    if (!rc) rc = upload(c, &c->d_dz, dz, nz_tap * sizeof(double));
+    const size_t ab = (size_t)nlines * ns * sizeof(double);
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_acc, ab);
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_comp, ab);
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_wp3d, ab);
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_wpx, ns * sizeof(double));
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_wpy, ns * sizeof(double));
+    if (!rc) rc = dev_alloc(c, (void**)&c->d_scratch, 4 * (size_t)ns * sizeof(double));
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->d_acc, 0, ab, c->own));
+    CK(cudaMemsetAsync(c->d_comp, 0, ab, c->own));
+    CK(cudaStreamSynchronize(c->own));
+    TapArgs& t = c->tap;
+    t.nlines = nlines;
+    t.base = c->d_base;
+    t.ns = ns;
+    t.nsteps = nsteps;
+    t.row_ptr = c->d_row;
+    t.ent_m = c->d_em;
+    t.ent_k0 = c->d_ek0;
+    t.ent_cnt = c->d_ecnt;
+    t.dz = c->d_dz;
+    t.acc = c->d_acc;
+    t.comp = c->d_comp;
+    return leave(c);
+}
+
+int fit_reset_wake(FitCtx* c) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->tap.nlines <= 0) return FIT_OK;
+    int rc = enter(c);
+    if (rc) return rc;
+    const size_t ab = (size_t)c->tap.nlines * c->tap.ns * sizeof(double);
+    CK(cudaMemsetAsync(c->d_acc, 0, ab, c->own));
+    CK(cudaMemsetAsync(c->d_comp, 0, ab, c->own));
+    return leave(c);
+}
+
+int fit_read_wake(FitCtx* c, double* out) {
+    if (!c || !out) return FIT_ERR_ARG;
+    if (c->tap.nlines <= 0) return fail(c, FIT_ERR_STATE, "no wake taps set");
+    int rc = enter(c);
+    if (rc) return rc;
+    const size_t n = (size_t)c->tap.nlines * c->tap.ns;
+    std::vector<double> a(n), b(n);
+    CK(cudaMemcpyAsync(a.data(), c->d_acc, n * sizeof(double), cudaMemcpyDeviceToHost, c->own));
+    CK(cudaMemcpyAsync(b.data(), c->d_comp, n * sizeof(double), cudaMemcpyDeviceToHost, c->own));
+    CK(cudaStreamSynchronize(c->own));
+    for (size_t i = 0; i < n; ++i) out[i] = a[i] + b[i];
+    return leave(c);
+}
+
+int fit_step(FitCtx* c, int64_t n, int32_t j_mode) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    const bool beam_off = (j_mode & FIT_STEP_NO_BEAM) != 0;
+    j_mode &= ~FIT_STEP_NO_BEAM;
+    int mode;
+    if (j_mode == FIT_J_EXPLICIT) {
+        if (!c->explicit_ready) return fail(c, FIT_ERR_STATE, "explicit-J storage not enabled");
+        mode = 2;
+    } else if (j_mode == FIT_J_ELIDED) {
+        mode = c->use_cond ? 1 : 0;
+    } else {
+        return fail(c, FIT_ERR_ARG, "bad j_mode %d", j_mode);
+    }
+    if (c->beam.active && !c->beam.dtieps) return fail(c, FIT_ERR_STATE, "beam set before coefficients");
+    rc = enter(c);
+    if (rc) return rc;
+    const int saved = c->beam.active;
+    if (beam_off) c->beam.active = 0;
+    launch_step(c, n, mode, false);
+    c->beam.active = saved;
+    return leave(c);
+}
+
+int fit_run(FitCtx* c, int64_t n0, int64_t nsteps) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (nsteps < 0) return fail(c, FIT_ERR_ARG, "nsteps < 0");
+    if (nsteps == 0) return FIT_OK;
+    if (c->beam.active && (c->vt_len < n0 + nsteps))
+        return fail(c, FIT_ERR_STATE, "beam vt table shorter than the run (%lld < %lld)", c->vt_len,
+                    (long long)(n0 + nsteps));
+    const int mode = c->use_cond ? 1 : 0;
+    rc = enter(c);
+    if (rc) return rc;
+    static thread_local long long host_n0;
+    host_n0 = n0;
+    CK(cudaMemcpyAsync(c->d_step, &host_n0, sizeof(long long), cudaMemcpyHostToDevice, c->own));
+    CK(cudaStreamSynchronize(c->own));
+    const long long chunk = 64;
+    if (nsteps >= chunk) {
+        if (!c->graph || c->graph_chunk != chunk) {
+            if (c->graph) {
+                cudaGraphExecDestroy(c->graph);
+                c->graph = nullptr;
+            }
+            cudaGraph_t gr;
+            CK(cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal));
+            c->capturing = true;
+            for (long long s = 0; s < chunk; ++s) launch_step(c, 0, mode, true);
+            c->capturing = false;
+            cudaError_t e = cudaStreamEndCapture(c->own, &gr);
+            if (e != cudaSuccess) return fail(c, FIT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&c->graph, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e != cudaSuccess) return fail(c, FIT_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+            c->graph_chunk = chunk;
+        }
+    }
+    long long done = 0;
+    while (nsteps - done >= chunk) {
+        CK(cudaGraphLaunch(c->graph, c->own));
+        g_launches += chunk * launches_per_step(c);
+        done += chunk;
+    }
+    for (; done < nsteps; ++done) launch_step(c, 0, mode, true);
+    return leave(c);
+}
+
+int fit_materialize_J(FitCtx* c, const double* sigma, int32_t flags) {
+    if (!c) return FIT_ERR_ARG;
+    const bool do_sig = (flags & 1) && c->use_cond;
+    const bool do_beam = (flags & 2) && c->beam.active;
+    if (do_sig && !sigma) return fail(c, FIT_ERR_ARG, "sigma required");
+    int rc = enter(c);
+    if (rc) return rc;
+    const long long n3 = 3 * c->g.N;
+    if (c->dtype == FIT_F64) {
+        if (do_sig) {
+            k_materialize_J<double><<<grid1d(n3, 256), 256, 0, c->own>>>((const double*)c->E, (double*)c->J, sigma, c->g, 1);
+            count(c);
+        }
+        if (do_beam) {
+            k_beam_line<double><<<grid1d(c->g.nz, 128), 128, 0, c->own>>>((double*)c->J, c->g, c->beam, c->beam_vt);
+            count(c);
+        }
+    } else {
+        if (do_sig) {
+            k_materialize_J<float><<<grid1d(n3, 256), 256, 0, c->own>>>((const float*)c->E, (float*)c->J, sigma, c->g, 1);
+            count(c);
+        }
+        if (do_beam) {
+            k_beam_line<float><<<grid1d(c->g.nz, 128), 128, 0, c->own>>>((float*)c->J, c->g, c->beam, c->beam_vt);
+            count(c);
+        }
+    }
+    return leave(c);
+}
+
+int fit_wake_finalize(FitCtx* c, double qscale, double ds, double dxf, double dyf, double* wp3d, double* wpx,
+                      double* wpy) {
+    if (!c || !wp3d) return FIT_ERR_ARG;
+    if (c->tap.nlines <= 0) return fail(c, FIT_ERR_STATE, "no wake taps set");
+    int rc = enter(c);
+    if (rc) return rc;
+    const int nl = c->tap.nlines, ns = c->tap.ns;
+    k_wake_finalize<<<1, 1024, 0, c->own>>>(c->d_acc, c->d_comp, nl, ns, qscale, ds, dxf, dyf, c->d_wp3d, c->d_wpx,
+                                            c->d_wpy, c->d_scratch);
+    g_launches++;
+    CK(cudaMemcpyAsync(wp3d, c->d_wp3d, (size_t)nl * ns * sizeof(double), cudaMemcpyDeviceToHost, c->own));
+    if (nl == 9 && wpx && wpy) {
+        CK(cudaMemcpyAsync(wpx, c->d_wpx, ns * sizeof(double), cudaMemcpyDeviceToHost, c->own));
+        CK(cudaMemcpyAsync(wpy, c->d_wpy, ns * sizeof(double), cudaMemcpyDeviceToHost, c->own));
+    }
+    CK(cudaStreamSynchronize(c->own));
+    return leave(c);
+}
+
+int fit_dft(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb, double* out) {
+    FitCtx* c = nullptr;
+    if (!x || !out || nsig <= 0 || len <= 0 || n <= 0 || nb <= 0 || b0 < 0)
+        return fail(nullptr, FIT_ERR_ARG, "bad fit_dft arguments");
+    const int nsplit = (int)std::max<long long>(1, std::min<long long>(32, len / 2048));
+    double* dx = nullptr;
+    double2* part = nullptr;
+    double2* dout = nullptr;
+    cudaStream_t s = nullptr;
+    auto cleanup = [&]() {
+        if (s) cudaStreamSynchronize(s);
+        dfree(dx);
+        dfree(part);
+        dfree(dout);
+        if (s) cudaStreamDestroy(s);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&dx, (size_t)nsig * len * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&part, (size_t)nsig * nsplit * nb * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)nsig * nb * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)nsig * len * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(nullptr, FIT_ERR_CUDA, "fit_dft setup failed: %s", cudaGetErrorString(e));
+    }
+    dim3 grid((unsigned)nb, (unsigned)nsig, (unsigned)nsplit);
+    k_dft_partial<<<grid, 256, 0, s>>>(dx, nsig, len, n, b0, nb, nsplit, part);
+    k_dft_reduce<<<grid1d((long long)nsig * nb, 256), 256, 0, s>>>(part, nsig, nb, nsplit, dout);
+    g_launches += 2;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, (size_t)nsig * nb * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cleanup();
+    if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "fit_dft failed: %s", cudaGetErrorString(e));
+    return FIT_OK;
+}
+
+int fit_version(char* buf, int64_t len) {
+    if (!buf || len <= 0) return FIT_ERR_ARG;
+    snprintf(buf, (size_t)len, "wakis_gb300 fit 0.1 sm_103a cuda %d", CUDART_VERSION);
+    return FIT_OK;
+}
+
+int64_t fit_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,752 @@
+// fit_kernels.cuh -- device code of the FIT leapfrog path for sm_103a.
+//
+// Field layout (shared with the Python Field class): a field is 3*N values, component
+// blocks [x | y | z], each block in Fortran order n = i + Nx*j + Nx*Ny*k.  The curl is
+// the reference's sparse matrix C (wakis/solverFIT3D.py:207-227) applied matrix-free:
+// forward differences D_a v[n] = v[n+s_a] - v[n] with v[n+s_a] = 0 past the end of the
+// block, and backward differences for C^T.  Neighbours follow the FLAT index, so at
+// i = Nx-1 the x neighbour of (i, j, k) is (0, j+1, k) and at j = Ny-1 the y neighbour
+// is (i, 0, k+1); the face masks zero those couplings for PEC/PML faces and leave them
+// live for periodic / ABC / open faces, exactly as the matrix does.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fit {
+
+// face bit f: 0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi, 4 z-lo, 5 z-hi
+struct Geom {
+    int nx, ny, nz;
+    int pad;
+    long long N;   // cells per component
+    long long sy;  // Nx
+    long long sz;  // Nx*Ny
+    unsigned pec;  // faces whose tangential E columns are zeroed (Dbc of PEC/PML)
+    unsigned pmc;  // faces whose tangential H rows/columns are zeroed (Dbc of PMC)
+};
+
+// Dbc face mask of component d at (i, j, k).  The reference writes the mask plane by
+// plane in the order x-lo, x-hi, y-lo, y-hi, z-lo, z-hi skipping the component's own
+// axis, so the LAST applicable write wins (wakis/boundaries.py:92-101): test in
+// reverse order.
+__device__ __forceinline__ bool face_open(unsigned bits, int d, int i, int j, int k, const Geom& g) {
+    if (bits == 0u) return true;
+    if (d != 2) {
+        if (k == g.nz - 1) return !((bits >> 5) & 1u);
+        if (k == 0) return !((bits >> 4) & 1u);
+    }
+    if (d != 1) {
+        if (j == g.ny - 1) return !((bits >> 3) & 1u);
+        if (j == 0) return !((bits >> 2) & 1u);
+    }
+    if (d != 0) {
+        if (i == g.nx - 1) return !((bits >> 1) & 1u);
+        if (i == 0) return !(bits & 1u);
+    }
+    return true;
+}
+
+template <typename T>
+struct Metric {
+    const T* L[3];   // primal edge lengths dx[i], dy[j], dz[k]
+    const T* tL[3];  // dual edge lengths after the periodic / ABC edits
+};
+
+// coordinate of a flat neighbour (flat-index semantics; valid = inside the block)
+struct Nb {
+    int i, j, k;
+    bool valid;
+};
+
+__device__ __forceinline__ Nb fwd_x(int i, int j, int k, const Geom& g) {
+    if (i + 1 < g.nx) return {i + 1, j, k, true};
+    if (j + 1 < g.ny) return {0, j + 1, k, true};
+    if (k + 1 < g.nz) return {0, 0, k + 1, true};
+    return {0, 0, 0, false};
+}
+__device__ __forceinline__ Nb fwd_y(int i, int j, int k, const Geom& g) {
+    if (j + 1 < g.ny) return {i, j + 1, k, true};
+    if (k + 1 < g.nz) return {i, 0, k + 1, true};
+    return {0, 0, 0, false};
+}
+__device__ __forceinline__ Nb fwd_z(int i, int j, int k, const Geom& g) {
+    if (k + 1 < g.nz) return {i, j, k + 1, true};
+    return {0, 0, 0, false};
+}
+__device__ __forceinline__ Nb bwd_x(int i, int j, int k, const Geom& g) {
+    if (i > 0) return {i - 1, j, k, true};
+    if (j > 0) return {g.nx - 1, j - 1, k, true};
+    if (k > 0) return {g.nx - 1, g.ny - 1, k - 1, true};
+    return {0, 0, 0, false};
+}
+__device__ __forceinline__ Nb bwd_y(int i, int j, int k, const Geom& g) {
+    if (j > 0) return {i, j - 1, k, true};
+    if (k > 0) return {i, g.ny - 1, k - 1, true};
+    return {0, 0, 0, false};
+}
+__device__ __forceinline__ Nb bwd_z(int i, int j, int k, const Geom& g) {
+    if (k > 0) return {i, j, k - 1, true};
+    return {0, 0, 0, false};
+}
+
+template <typename T>
+__device__ __forceinline__ T edge_len(const T* const* L, int d, int i, int j, int k) {
+    return d == 0 ? L[0][i] : (d == 1 ? L[1][j] : L[2][k]);
+}
+
+// ê_d(m) = Dbc_pec * L_d * E_d[m]  (column scaling of C by Ds and Dbc)
+template <typename T>
+__device__ __forceinline__ T ehat(T e, int d, const Nb& p, const Geom& g, const Metric<T>& m) {
+    if (!p.valid) return T(0);
+    if (!face_open(g.pec, d, p.i, p.j, p.k, g)) return T(0);
+    return edge_len<T>(m.L, d, p.i, p.j, p.k) * e;
+}
+// ĥ_d(m) = Dbc_pmc * tL_d * H_d[m]
+template <typename T>
+__device__ __forceinline__ T hhat(T h, int d, const Nb& p, const Geom& g, const Metric<T>& m) {
+    if (!p.valid) return T(0);
+    if (!face_open(g.pmc, d, p.i, p.j, p.k, g)) return T(0);
+    return edge_len<T>(m.tL, d, p.i, p.j, p.k) * h;
+}
+
+// ---------------------------------------------------------------- vector loads/stores
+template <typename T, int VEC>
+__device__ __forceinline__ void ldg_v(T (&r)[VEC], const T* __restrict__ p) {
+    if constexpr (VEC == 4 && sizeof(T) == 4) {
+        float4 t = __ldg(reinterpret_cast<const float4*>(p));
+        r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
+    } else if constexpr (VEC == 2 && sizeof(T) == 8) {
+        double2 t = __ldg(reinterpret_cast<const double2*>(p));
+        r[0] = t.x; r[1] = t.y;
+    } else if constexpr (VEC == 2 && sizeof(T) == 4) {
+        float2 t = __ldg(reinterpret_cast<const float2*>(p));
+        r[0] = t.x; r[1] = t.y;
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) r[e] = __ldg(p + e);
+    }
+}
+template <typename T, int VEC>
+__device__ __forceinline__ void ld_v(T (&r)[VEC], const T* p) {
+    if constexpr (VEC == 4 && sizeof(T) == 4) {
+        float4 t = *reinterpret_cast<const float4*>(p);
+        r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
+    } else if constexpr (VEC == 2 && sizeof(T) == 8) {
+        double2 t = *reinterpret_cast<const double2*>(p);
+        r[0] = t.x; r[1] = t.y;
+    } else if constexpr (VEC == 2 && sizeof(T) == 4) {
+        float2 t = *reinterpret_cast<const float2*>(p);
+        r[0] = t.x; r[1] = t.y;
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) r[e] = p[e];
+    }
+}
+template <typename T, int VEC>
+__device__ __forceinline__ void st_v(T* p, const T (&r)[VEC]) {
+    if constexpr (VEC == 4 && sizeof(T) == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
+    } else if constexpr (VEC == 2 && sizeof(T) == 8) {
+        *reinterpret_cast<double2*>(p) = make_double2(r[0], r[1]);
+    } else if constexpr (VEC == 2 && sizeof(T) == 4) {
+        *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) p[e] = r[e];
+    }
+}
+template <typename T, int VEC>
+__device__ __forceinline__ void zero_v(T (&r)[VEC]) {
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r[e] = T(0);
+}
+
+// ---------------------------------------------------------------- beam line current
+// sources.Beam.update (wakis/sources.py:98-110), evaluated in FP64 with the reference's
+// operation order:  J = ((q*v)*profile)/dx/dy,
+//   profile = (1/sqrt(2*pi*sigmaz^2)) * exp(-((z - vt) - s0)^2 / (2*sigmaz^2)).
+struct BeamArgs {
+    int active;
+    int ixs, iys;
+    double qv;        // q*v
+    double c0;        // 1/sqrt(2*pi*sigmaz^2)
+    double two_s2;    // 2*sigmaz^2
+    double s0;        // zmin - v*ti
+    double dx_s, dy_s;
+    const double* z;  // cell-centre z, nz values
+    const double* dtieps;  // dt*ieps_z on the line, nz values (FP64)
+};
+
+__device__ __forceinline__ double beam_current(const BeamArgs& b, int k, double vt) {
+    double s = __dsub_rn(b.z[k], vt);
+    double d = __dsub_rn(s, b.s0);
+    double prof = __dmul_rn(b.c0, exp(-__dmul_rn(d, d) / b.two_s2));
+    return __dmul_rn(b.qv, prof) / b.dx_s / b.dy_s;
+}
+
+// step number / beam position of a launch: host-driven launches pass them as values;
+// graph-replayed launches read the step counter on the device.
+struct StepArgs {
+    long long n;
+    double vt;
+    const long long* d_step;  // if set: n = *d_step - 1 (the prologue already advanced it)
+    const double* vt_table;   // with d_step: vt = vt_table[n]
+    long long vt_len;
+};
+
+__device__ __forceinline__ void resolve_step(const StepArgs& s, long long& n, double& vt) {
+    if (s.d_step) {
+        n = *s.d_step - 1;
+        vt = (s.vt_table && n >= 0 && n < s.vt_len) ? s.vt_table[n] : 0.0;
+    } else {
+        n = s.n;
+        vt = s.vt;
+    }
+}
+
+struct PlaneArgs {
+    int active;
+    int zs, x0, x1, y0, y1;
+    const double* prof;  // (x1-x0)*(y1-y0) or null
+    const double* c1;
+    const double* c2;
+    const double* gt;
+    long long len;
+    double* stash;  // E_x of the plane before the source overwrote it (loss term)
+};
+
+// ---------------------------------------------------------------- H pass
+// H_c <- H_c - ch_c * (C ê)_c, one thread per VEC consecutive x cells.
+template <typename T, int VEC>
+__global__ void __launch_bounds__(256) k_hpass(const T* __restrict__ E, T* __restrict__ H,
+                                               const T* __restrict__ ch, Geom g, Metric<T> mt) {
+    const long long nvec = g.N / VEC;
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvec) return;
+    const long long n = v * VEC;
+    const int i0 = (int)(n % g.nx);
+    const long long r = n / g.nx;
+    const int j = (int)(r % g.ny);
+    const int k = (int)(r / g.ny);
+    const T* Ex = E;
+    const T* Ey = E + g.N;
+    const T* Ez = E + 2 * g.N;
+
+    T ex[VEC], ey[VEC], ez[VEC];
+    ldg_v<T, VEC>(ex, Ex + n);
+    ldg_v<T, VEC>(ey, Ey + n);
+    ldg_v<T, VEC>(ez, Ez + n);
+    // y-forward row (n + Nx) and z-forward plane (n + Nx*Ny)
+    const bool yv = (j + 1 < g.ny) || (k + 1 < g.nz);
+    const bool zv = (k + 1 < g.nz);
+    T exy[VEC], ezy[VEC], exz[VEC], eyz[VEC];
+    if (yv) {
+        ldg_v<T, VEC>(exy, Ex + n + g.sy);
+        ldg_v<T, VEC>(ezy, Ez + n + g.sy);
+    } else {
+        zero_v<T, VEC>(exy);
+        zero_v<T, VEC>(ezy);
+    }
+    if (zv) {
+        ldg_v<T, VEC>(exz, Ex + n + g.sz);
+        ldg_v<T, VEC>(eyz, Ey + n + g.sz);
+    } else {
+        zero_v<T, VEC>(exz);
+        zero_v<T, VEC>(eyz);
+    }
+    // x-forward of the last element
+    const Nb xl = fwd_x(i0 + VEC - 1, j, k, g);
+    T eyx = T(0), ezx = T(0);
+    if (xl.valid) {
+        eyx = __ldg(Ey + n + VEC);
+        ezx = __ldg(Ez + n + VEC);
+    }
+
+    T hx[VEC], hy[VEC], hz[VEC], cx[VEC], cy[VEC], cz[VEC];
+    ld_v<T, VEC>(hx, H + n);
+    ld_v<T, VEC>(hy, H + g.N + n);
+    ld_v<T, VEC>(hz, H + 2 * g.N + n);
+    ldg_v<T, VEC>(cx, ch + n);
+    ldg_v<T, VEC>(cy, ch + g.N + n);
+    ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
+
+    const Nb py = fwd_y(i0, j, k, g);  // i replaced per element below
+    const Nb pz = fwd_z(i0, j, k, g);
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+        const int i = i0 + e;
+        const Nb p0{i, j, k, true};
+        const Nb pyi{i, py.j, py.k, py.valid};
+        const Nb pzi{i, pz.j, pz.k, pz.valid};
+        const Nb pxi = (e + 1 < VEC) ? Nb{i + 1, j, k, true} : xl;
+        const T ex0 = ehat<T>(ex[e], 0, p0, g, mt);
+        const T ey0 = ehat<T>(ey[e], 1, p0, g, mt);
+        const T ez0 = ehat<T>(ez[e], 2, p0, g, mt);
+        const T exY = ehat<T>(exy[e], 0, pyi, g, mt);
+        const T ezY = ehat<T>(ezy[e], 2, pyi, g, mt);
+        const T exZ = ehat<T>(exz[e], 0, pzi, g, mt);
+        const T eyZ = ehat<T>(eyz[e], 1, pzi, g, mt);
+        const T eyX = ehat<T>((e + 1 < VEC) ? ey[e + 1] : eyx, 1, pxi, g, mt);
+        const T ezX = ehat<T>((e + 1 < VEC) ? ez[e + 1] : ezx, 2, pxi, g, mt);
+        // (C ê)_x = -D_z ê_y + D_y ê_z ; (C ê)_y = D_z ê_x - D_x ê_z ; (C ê)_z = -D_y ê_x + D_x ê_y
+        const T curlx = (ey0 - eyZ) + (ezY - ez0);
+        const T curly = (exZ - ex0) + (ez0 - ezX);
+        const T curlz = (ex0 - exY) + (eyX - ey0);
+        hx[e] = hx[e] - cx[e] * curlx;
+        hy[e] = hy[e] - cy[e] * curly;
+        hz[e] = hz[e] - cz[e] * curlz;
+    }
+    st_v<T, VEC>(H + n, hx);
+    st_v<T, VEC>(H + g.N + n, hy);
+    st_v<T, VEC>(H + 2 * g.N + n, hz);
+}
+
+// ---------------------------------------------------------------- E pass
+// MODE 0: E += ce*(C^T ĥ)                       (no conduction current)
+// MODE 1: E = cl*E + ce*(C^T ĥ)                 (J = sigma*E_prev folded into cl)
+// MODE 2: E = E + ce*(C^T ĥ) - cj*J; J = sg*E   (explicit J; J written if conductive)
+// The beam line (ixs, iys, :) of the z component uses the beam current instead of J.
+template <typename T, int VEC, int MODE>
+__global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __restrict__ H,
+                                               const T* __restrict__ ce, const T* __restrict__ cl,
+                                               T* __restrict__ J, const T* __restrict__ cj,
+                                               const T* __restrict__ sg, int use_cond, Geom g,
+                                               Metric<T> mt, BeamArgs b, PlaneArgs pl, StepArgs st) {
+    const long long nvec = g.N / VEC;
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvec) return;
+    const long long n = v * VEC;
+    const int i0 = (int)(n % g.nx);
+    const long long r = n / g.nx;
+    const int j = (int)(r % g.ny);
+    const int k = (int)(r / g.ny);
+    const T* Hx = H;
+    const T* Hy = H + g.N;
+    const T* Hz = H + 2 * g.N;
+
+    T hx[VEC], hy[VEC], hz[VEC];
+    ldg_v<T, VEC>(hx, Hx + n);
+    ldg_v<T, VEC>(hy, Hy + n);
+    ldg_v<T, VEC>(hz, Hz + n);
+    const bool yv = (j > 0) || (k > 0);
+    const bool zv = (k > 0);
+    T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
+    if (yv) {
+        ldg_v<T, VEC>(hxy, Hx + n - g.sy);
+        ldg_v<T, VEC>(hzy, Hz + n - g.sy);
+    } else {
+        zero_v<T, VEC>(hxy);
+        zero_v<T, VEC>(hzy);
+    }
+    if (zv) {
+        ldg_v<T, VEC>(hxz, Hx + n - g.sz);
+        ldg_v<T, VEC>(hyz, Hy + n - g.sz);
+    } else {
+        zero_v<T, VEC>(hxz);
+        zero_v<T, VEC>(hyz);
+    }
+    const Nb xf = bwd_x(i0, j, k, g);
+    T hyx = T(0), hzx = T(0);
+    if (xf.valid) {
+        hyx = __ldg(Hy + n - 1);
+        hzx = __ldg(Hz + n - 1);
+    }
+
+    T ex[VEC], ey[VEC], ez[VEC], kx[VEC], ky[VEC], kz[VEC];
+    ld_v<T, VEC>(ex, E + n);
+    ld_v<T, VEC>(ey, E + g.N + n);
+    ld_v<T, VEC>(ez, E + 2 * g.N + n);
+    ldg_v<T, VEC>(kx, ce + n);
+    ldg_v<T, VEC>(ky, ce + g.N + n);
+    ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+
+    const Nb py = bwd_y(i0, j, k, g);
+    const Nb pz = bwd_z(i0, j, k, g);
+    T cur[3][VEC];
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+        const int i = i0 + e;
+        const Nb p0{i, j, k, true};
+        const Nb pyi{i, py.j, py.k, py.valid};
+        const Nb pzi{i, pz.j, pz.k, pz.valid};
+        const Nb pxi = (e > 0) ? Nb{i - 1, j, k, true} : xf;
+        const T hx0 = hhat<T>(hx[e], 0, p0, g, mt);
+        const T hy0 = hhat<T>(hy[e], 1, p0, g, mt);
+        const T hz0 = hhat<T>(hz[e], 2, p0, g, mt);
+        const T hxY = hhat<T>(hxy[e], 0, pyi, g, mt);
+        const T hzY = hhat<T>(hzy[e], 2, pyi, g, mt);
+        const T hxZ = hhat<T>(hxz[e], 0, pzi, g, mt);
+        const T hyZ = hhat<T>(hyz[e], 1, pzi, g, mt);
+        const T hyX = hhat<T>((e > 0) ? hy[e - 1] : hyx, 1, pxi, g, mt);
+        const T hzX = hhat<T>((e > 0) ? hz[e - 1] : hzx, 2, pxi, g, mt);
+        // (C^T ĥ)_x = D^T_z ĥ_y - D^T_y ĥ_z ; (C^T ĥ)_y = -D^T_z ĥ_x + D^T_x ĥ_z ;
+        // (C^T ĥ)_z = D^T_y ĥ_x - D^T_x ĥ_y   with D^T_a v[m] = v[m - s_a] - v[m]
+        cur[0][e] = (hyZ - hy0) + (hz0 - hzY);
+        cur[1][e] = (hx0 - hxZ) + (hzX - hz0);
+        cur[2][e] = (hxY - hx0) + (hy0 - hyX);
+    }
+
+    // beam line of the z component
+    const bool on_line = b.active && (j == b.iys) && (b.ixs >= i0) && (b.ixs < i0 + VEC);
+    double jb = 0.0;
+    if (on_line) {
+        long long sn;
+        double vt;
+        resolve_step(st, sn, vt);
+        jb = beam_current(b, k, vt);
+    }
+
+    if constexpr (MODE == 0) {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            ex[e] = ex[e] + kx[e] * cur[0][e];
+            ey[e] = ey[e] + ky[e] * cur[1][e];
+            ez[e] = ez[e] + kz[e] * cur[2][e];
+        }
+    } else if constexpr (MODE == 1) {
+        T lx[VEC], ly[VEC], lz[VEC];
+        ldg_v<T, VEC>(lx, cl + n);
+        ldg_v<T, VEC>(ly, cl + g.N + n);
+        ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+        // on the hard-source plane the conduction current is sigma times the E_x the
+        // source overwrote (J was computed at the end of the previous step)
+        const bool on_plane = pl.active && k == pl.zs && j >= pl.y0 && j < pl.y1;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int i = i0 + e;
+            if (on_plane && i >= pl.x0 && i < pl.x1)
+                ex[e] = (ex[e] - (T(1) - lx[e]) * (T)pl.stash[(i - pl.x0) + (j - pl.y0) * (pl.x1 - pl.x0)]) +
+                        kx[e] * cur[0][e];
+            else
+                ex[e] = lx[e] * ex[e] + kx[e] * cur[0][e];
+            ey[e] = ly[e] * ey[e] + ky[e] * cur[1][e];
+            // on the beam line J was overwritten by the beam: no sigma*E term there
+            ez[e] = ((on_line && (i0 + e == b.ixs)) ? ez[e] : lz[e] * ez[e]) + kz[e] * cur[2][e];
+        }
+    } else {
+        T jx[VEC], jy[VEC], jz[VEC], ax[VEC], ay[VEC], az[VEC];
+        ld_v<T, VEC>(jx, J + n);
+        ld_v<T, VEC>(jy, J + g.N + n);
+        ld_v<T, VEC>(jz, J + 2 * g.N + n);
+        ldg_v<T, VEC>(ax, cj + n);
+        ldg_v<T, VEC>(ay, cj + g.N + n);
+        ldg_v<T, VEC>(az, cj + 2 * g.N + n);
+        if (on_line) jz[b.ixs - i0] = (T)jb;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            ex[e] = ex[e] + kx[e] * cur[0][e] - ax[e] * jx[e];
+            ey[e] = ey[e] + ky[e] * cur[1][e] - ay[e] * jy[e];
+            ez[e] = ez[e] + kz[e] * cur[2][e] - az[e] * jz[e];
+        }
+        if (use_cond) {
+            T sx[VEC], sy_[VEC], szz[VEC];
+            ldg_v<T, VEC>(sx, sg + n);
+            ldg_v<T, VEC>(sy_, sg + g.N + n);
+            ldg_v<T, VEC>(szz, sg + 2 * g.N + n);
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                jx[e] = sx[e] * ex[e];
+                jy[e] = sy_[e] * ey[e];
+                jz[e] = szz[e] * ez[e];
+            }
+            st_v<T, VEC>(J + n, jx);
+            st_v<T, VEC>(J + g.N + n, jy);
+            st_v<T, VEC>(J + 2 * g.N + n, jz);
+        } else if (on_line) {
+            J[2 * g.N + n + (b.ixs - i0)] = (T)jb;
+        }
+    }
+    if constexpr (MODE != 2) {
+        if (on_line) {
+            const int e = b.ixs - i0;
+            ez[e] = ez[e] - (T)b.dtieps[k] * (T)jb;
+            if (!use_cond) J[2 * g.N + n + e] = (T)jb;  // J keeps the last beam value
+        }
+    }
+    st_v<T, VEC>(E + n, ex);
+    st_v<T, VEC>(E + g.N + n, ey);
+    st_v<T, VEC>(E + 2 * g.N + n, ez);
+}
+
+// ---------------------------------------------------------------- coefficients
+// FP64 build of ch, ce, cl (+ cj, sg for the explicit-J pass) from the material tensors.
+// iA_c = 1/(L_p L_q) (wakis/gridFIT3D.py:277-280); itA_c = 1/(tL_p tL_q) or 0 where the
+// dual area is 0 (wakis/gridFIT3D.py:298-304), then the periodic / ABC edits of
+// wakis/boundaries.py:36-70,153-181 in the order they are applied: an edit along axis a
+// sets itA_c(last index along a) = iA_c(index 0 along a) for c != a; the last edit wins.
+struct CoeffArgs {
+    const double* L[3];   // dx, dy, dz (FP64)
+    const double* tL[3];  // UNEDITED dual lengths (FP64)
+    int edits[6];         // axes in application order
+    int n_edits;
+    double dt;
+    int use_cond;
+};
+
+__device__ __forceinline__ double coord_len(const double* const* L, int a, int i, int j, int k) {
+    return a == 0 ? L[0][i] : (a == 1 ? L[1][j] : L[2][k]);
+}
+
+template <typename T>
+__global__ void k_build_coeffs(const double* __restrict__ ieps, const double* __restrict__ imu,
+                               const double* __restrict__ sigma, T* __restrict__ ch, T* __restrict__ ce,
+                               T* __restrict__ cl, T* __restrict__ cj, T* __restrict__ sg, Geom g,
+                               CoeffArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * g.N) return;
+    const int c = (int)(idx / g.N);
+    const long long n = idx - (long long)c * g.N;
+    const int i = (int)(n % g.nx);
+    const long long r = n / g.nx;
+    const int j = (int)(r % g.ny);
+    const int k = (int)(r / g.ny);
+    const int p = (c + 1) % 3, q = (c + 2) % 3;  // the two other axes
+    // primal inverse area
+    const double iA = 1.0 / (coord_len(a.L, p, i, j, k) * coord_len(a.L, q, i, j, k));
+    // dual inverse area with edits
+    double itA;
+    int edit_axis = -1;
+    for (int e = a.n_edits - 1; e >= 0; --e) {
+        const int ax = a.edits[e];
+        if (ax == c) continue;
+        const int last = ax == 0 ? g.nx - 1 : (ax == 1 ? g.ny - 1 : g.nz - 1);
+        const int cur = ax == 0 ? i : (ax == 1 ? j : k);
+        if (cur == last) {
+            edit_axis = ax;
+            break;
+        }
+    }
+    if (edit_axis >= 0) {
+        const int i2 = edit_axis == 0 ? 0 : i, j2 = edit_axis == 1 ? 0 : j, k2 = edit_axis == 2 ? 0 : k;
+        itA = 1.0 / (coord_len(a.L, p, i2, j2, k2) * coord_len(a.L, q, i2, j2, k2));
+    } else {
+        const double ar = coord_len(a.tL, p, i, j, k) * coord_len(a.tL, q, i, j, k);
+        itA = ar != 0.0 ? 1.0 / ar : 0.0;
+    }
+    const double pec = face_open(g.pec, c, i, j, k, g) ? 1.0 : 0.0;
+    const double pmc = face_open(g.pmc, c, i, j, k, g) ? 1.0 : 0.0;
+    const double ie = ieps[idx];
+    ch[idx] = (T)(a.dt * (iA * imu[idx]) * pmc);
+    ce[idx] = (T)(a.dt * (ie * itA) * pec);
+    if (cl) cl[idx] = (T)(1.0 - a.dt * ie * sigma[idx]);
+    if (cj) cj[idx] = (T)(a.dt * ie);
+    if (sg) sg[idx] = (T)sigma[idx];
+}
+
+// ---------------------------------------------------------------- small kernels
+template <typename T>
+__global__ void k_zero_ghosts(T* __restrict__ E, T* __restrict__ H, Geom g) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.N) return;
+    const int i = (int)(n % g.nx);
+    const long long r = n / g.nx;
+    const int j = (int)(r % g.ny);
+    const int k = (int)(r / g.ny);
+    const bool xl = i == g.nx - 1, yl = j == g.ny - 1, zl = k == g.nz - 1;
+    if (yl || zl) H[n] = T(0);
+    if (xl || zl) H[g.N + n] = T(0);
+    if (xl || yl) H[2 * g.N + n] = T(0);
+    if (xl) E[n] = T(0);
+    if (yl) E[g.N + n] = T(0);
+    if (zl) E[2 * g.N + n] = T(0);
+}
+
+// copy the index-1 plane to the index-0 plane along `axis`, all components of E and H
+template <typename T>
+__global__ void k_abc_lo(T* __restrict__ E, T* __restrict__ H, Geom g, int axis) {
+    const int pa = axis == 0 ? g.ny : g.nx;
+    const int pb = axis == 2 ? g.ny : g.nz;
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= 6LL * pa * pb) return;
+    const int f = (int)(m / ((long long)pa * pb));
+    const long long q = m - (long long)f * pa * pb;
+    const int u = (int)(q % pa), w = (int)(q / pa);
+    int i, j, k;
+    long long s;
+    if (axis == 0) { i = 0; j = u; k = w; s = 1; }
+    else if (axis == 1) { i = u; j = 0; k = w; s = g.sy; }
+    else { i = u; j = w; k = 0; s = g.sz; }
+    T* F = (f < 3 ? E : H) + (long long)(f % 3) * g.N;
+    const long long n = i + g.sy * j + g.sz * k;
+    F[n] = F[n + s];
+}
+
+// hard plane source + wake taps + step counter (one launch per step, before the H pass)
+struct TapArgs {
+    int nlines;
+    const long long* base;  // flat index of E_z(lx, ly, kskip) per line
+    int ns;
+    long long nsteps;
+    const long long* row_ptr;
+    const int* ent_m;
+    const int* ent_k0;
+    const int* ent_cnt;
+    const double* dz;
+    double* acc;   // nlines*ns running sums
+    double* comp;  // nlines*ns Neumaier compensation
+};
+
+__device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
+template <typename T>
+__global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneArgs pl, TapArgs tp,
+                           long long n_arg, long long* d_step) {
+    const long long n = d_step ? *d_step : n_arg;
+    // plane source
+    if (pl.active && n >= 0 && n < pl.len) {
+        const int w = pl.x1 - pl.x0, h = pl.y1 - pl.y0;
+        const double c1 = pl.c1[n], c2 = pl.c2[n], gt = pl.gt[n];
+        for (int t = threadIdx.x; t < w * h; t += blockDim.x) {
+            const int i = pl.x0 + t % w, j = pl.y0 + t / w;
+            const double pv = pl.prof ? pl.prof[t] : 1.0;
+            const long long c = i + g.sy * j + g.sz * pl.zs;
+            if (pl.stash) pl.stash[t] = (double)E[c];
+            H[g.N + c] = (T)__dmul_rn(__dmul_rn(c1, pv), gt);
+            E[c] = (T)__dmul_rn(__dmul_rn(c2, pv), gt);
+        }
+    }
+    // wake taps of E^n
+    if (tp.nlines > 0 && n >= 0 && n < tp.nsteps) {
+        const long long r0 = tp.row_ptr[n], r1 = tp.row_ptr[n + 1];
+        const long long cnt = (r1 - r0) * tp.nlines;
+        const T* Ez = E + 2 * g.N;
+        for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const long long e = r0 + t / tp.nlines;
+            const int l = (int)(t % tp.nlines);
+            const int m = tp.ent_m[e], k0 = tp.ent_k0[e], c = tp.ent_cnt[e];
+            double s = tp.acc[(long long)l * tp.ns + m], cc = tp.comp[(long long)l * tp.ns + m];
+            for (int q = 0; q < c; ++q) {
+                const double ez = (double)Ez[tp.base[l] + g.sz * (long long)(k0 + q)];
+                neumaier_add(s, cc, __dmul_rn(ez, tp.dz[k0 + q]));
+            }
+            tp.acc[(long long)l * tp.ns + m] = s;
+            tp.comp[(long long)l * tp.ns + m] = cc;
+        }
+    }
+    if (d_step) {
+        __syncthreads();
+        if (threadIdx.x == 0) *d_step = n + 1;
+    }
+}
+
+// J = sigma*E (field dtype) and the beam line
+template <typename T>
+__global__ void k_materialize_J(const T* __restrict__ E, T* __restrict__ J, const double* __restrict__ sigma,
+                                Geom g, int use_cond) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * g.N) return;
+    if (use_cond) J[idx] = (T)sigma[idx] * E[idx];
+}
+template <typename T>
+__global__ void k_beam_line(T* __restrict__ J, Geom g, BeamArgs b, double vt) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= g.nz) return;
+    J[2 * g.N + b.ixs + g.sy * b.iys + g.sz * k] = (T)beam_current(b, k, vt);
+}
+
+// wake post-processing: combine lines with the non-reset accumulator of the reference,
+// then exclusive prefix sums (x ds) and the Panofsky-Wenzel central differences.
+// One block of 1024 threads.
+__global__ void k_wake_finalize(const double* __restrict__ acc, const double* __restrict__ comp, int nlines,
+                                int ns, double qscale, double ds, double dxf, double dyf,
+                                double* __restrict__ wp3d, double* __restrict__ wpx, double* __restrict__ wpy,
+                                double* __restrict__ scratch /* 4*ns */) {
+    // 1. line combination, sequential over lines, parallel over s
+    for (int m = threadIdx.x; m < ns; m += blockDim.x) {
+        double prev = 0.0;
+        for (int l = 0; l < nlines; ++l) {
+            const double raw = acc[(long long)l * ns + m] + comp[(long long)l * ns + m];
+            prev = (prev + raw) / qscale;
+            wp3d[(long long)l * ns + m] = prev;
+        }
+    }
+    __syncthreads();
+    if (nlines != 9) return;
+    // 2. exclusive prefix sums of lines (2,1)->7, (0,1)->1, (1,2)->5, (1,0)->3 (row-major 3x3)
+    __shared__ double part[1024];
+    const int lines[4] = {7, 1, 5, 3};
+    const int T = blockDim.x;
+    const int chunk = (ns + T - 1) / T;
+    for (int q = 0; q < 4; ++q) {
+        const double* w = wp3d + (long long)lines[q] * ns;
+        const int a = threadIdx.x * chunk, bnd = min(ns, a + chunk);
+        double s = 0.0, c = 0.0;
+        for (int m = a; m < bnd; ++m) neumaier_add(s, c, w[m]);
+        part[threadIdx.x] = s + c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double run = 0.0, rc = 0.0;
+            for (int t = 0; t < T; ++t) {
+                const double v = part[t];
+                part[t] = run + rc;
+                neumaier_add(run, rc, v);
+            }
+        }
+        __syncthreads();
+        s = part[threadIdx.x];
+        c = 0.0;
+        for (int m = a; m < bnd; ++m) {
+            scratch[(long long)q * ns + m] = (s + c) * ds;  // sum of w[0:m]
+            neumaier_add(s, c, w[m]);
+        }
+        __syncthreads();
+    }
+    for (int m = threadIdx.x; m < ns; m += blockDim.x) {
+        wpx[m] = -(scratch[m] - scratch[ns + m]) / dxf;
+        wpy[m] = -(scratch[2LL * ns + m] - scratch[3LL * ns + m]) / dyf;
+    }
+}
+
+// FP64 direct DFT: stage 1 writes compensated partial sums of a slice of the time axis
+// to scratch; stage 2 adds the slices.  Twiddle phase from the exact integer (b*t) mod n.
+__global__ void k_dft_partial(const double* __restrict__ x, int nsig, long long len, long long n, long long b0,
+                              int nb, int nsplit, double2* __restrict__ part) {
+    const int b = blockIdx.x;          // bin offset
+    const int sgl = blockIdx.y;        // signal
+    const int sp = blockIdx.z;         // slice
+    const long long per = (len + nsplit - 1) / nsplit;
+    const long long t0 = (long long)sp * per, t1 = min(len, t0 + per);
+    const long long bin = b0 + b;
+    double sr = 0.0, cr = 0.0, si = 0.0, ci = 0.0;
+    const double* xs = x + (long long)sgl * len;
+    for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        const long long rr = (long long)(((unsigned long long)bin * (unsigned long long)t) % (unsigned long long)n);
+        double sn, cs;
+        sincospi(2.0 * (double)rr / (double)n, &sn, &cs);
+        const double v = xs[t];
+        neumaier_add(sr, cr, v * cs);
+        neumaier_add(si, ci, -v * sn);
+    }
+    __shared__ double red_r[256], red_i[256];
+    red_r[threadIdx.x] = sr + cr;
+    red_i[threadIdx.x] = si + ci;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red_r[threadIdx.x] += red_r[threadIdx.x + w];
+            red_i[threadIdx.x] += red_i[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[((long long)sgl * nsplit + sp) * nb + b] = make_double2(red_r[0], red_i[0]);
+}
+
+__global__ void k_dft_reduce(const double2* __restrict__ part, int nsig, int nb, int nsplit, double2* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nsig * nb) return;
+    const int sgl = (int)(idx / nb), b = (int)(idx % nb);
+    double sr = 0.0, cr = 0.0, si = 0.0, ci = 0.0;
+    for (int sp = 0; sp < nsplit; ++sp) {
+        const double2 v = part[((long long)sgl * nsplit + sp) * nb + b];
+        neumaier_add(sr, cr, v.x);
+        neumaier_add(si, ci, v.y);
+    }
+    out[idx] = make_double2(sr + cr, si + ci);
+}
+
+}  // namespace fit

@@ -1,0 +1,224 @@
+"""Time-loop drivers emsolve / wakesolve (wakis/routines.py:17-485).
+
+wakesolve: instead of dumping the 3x3xNz Ez slab to HDF5 every step and integrating it
+in Python afterwards, the Ez line integral of the wake potential is accumulated on the
+device while the loop runs (FP64, compensated); the tap table (which step feeds which
+(s, z) pair) is derived on the host with the post-processor's own expressions, so the
+index set is the one WakeSolver.calc_long_WP_3d would use.  The beam current is
+evaluated inside the E pass.  Without per-step Python work (no callback, plot or field
+monitor) the whole loop runs as CUDA-graph replays with the step number on the device.
+
+emsolve: a PlaneWave / WavePacket source is replayed on the device from per-step
+tables; other sources, callbacks and saving run the loop step by step.
+"""
+
+import time
+
+import numpy as np
+
+from . import _native as nat
+from .sources import Beam, PlaneWave, WavePacket
+
+
+def _step_times(dt, n):
+    """t = n*dt for n = 0..n-1 with the scalar types of the reference's `n * self.dt`."""
+    if isinstance(dt, np.float32):
+        return np.arange(n).astype(np.float32) * dt
+    return np.arange(n) * dt
+
+
+class RoutinesMixin:
+    # ------------------------------------------------------------------ emsolve
+    def emsolve(self, Nt, source=None, callback=None, save=False, fields=["E"], components=["Abs"], save_every=1,
+                subdomain=None, plot=False, plot_every=1, use_etd=False, plot3d=False, **kwargs):
+        self.Nt = Nt
+        if source is not None:
+            self.source = source
+        if plot or plot3d:
+            raise NotImplementedError("plotting is not provided")
+        hfs = None
+        if save:
+            hfs = self._open_saves(Nt, fields, components, save_every, subdomain)
+        abc_axes = self._abc_lo_axes() if self.activate_abc else 0
+        self._ctx.call("fit_set_abc", abc_axes)
+        try:
+            fast = (callback is None and not save and type(source) in (PlaneWave, WavePacket))
+            if fast and Nt > 0:
+                self._emsolve_device(Nt, source)
+            else:
+                for n in range(Nt):
+                    if source is not None:
+                        source.update(self, n * self.dt)
+                    if save and n % save_every == 0:
+                        self._save_step(hfs, n)
+                    self.one_step()
+                    if callback is not None:
+                        callback(self, n * self.dt)
+        finally:
+            self._ctx.call("fit_set_abc", 0)
+            if hfs is not None:
+                self._close_saves(hfs)
+
+    def _emsolve_device(self, Nt, source):
+        if source.is_first_update:
+            source._first(self)
+        w = (source.xs.stop if source.xs.stop is not None else self.Nx) - (source.xs.start or 0)
+        h = (source.ys.stop if source.ys.stop is not None else self.Ny) - (source.ys.start or 0)
+        x0, y0 = source.xs.start or 0, source.ys.start or 0
+        if (source.xs.step not in (None, 1)) or (source.ys.step not in (None, 1)) or not isinstance(source.zs, (int, np.integer)):
+            # strided or multi-plane sources: step by step through the Field API
+            for n in range(Nt):
+                source.update(self, n * self.dt)
+                self.one_step()
+            return
+        prof = source.profile(self)
+        prof_arr = None
+        if prof is not None:
+            prof_arr = np.ascontiguousarray(np.broadcast_to(np.asarray(prof, dtype=np.float64), (w, h)).ravel(order="F"))
+        tabs = np.array([source.factors(self, n * self.dt) for n in range(Nt)], dtype=np.float64)
+        c1, c2, gt = (np.ascontiguousarray(tabs[:, i]) for i in range(3))
+        # the first step goes through the Field API as in the reference (source write,
+        # then ghost zeroing, then the explicit-J pass if J is not sigma*E yet)
+        n0 = self.nstep
+        source.update(self, 0 * self.dt)
+        self._advance(0)
+        if Nt == 1:
+            return
+        self._ctx.call("fit_set_plane_source", 1, int(source.zs), int(x0), int(x0 + w), int(y0), int(y0 + h),
+                       nat.dptr(prof_arr) if prof_arr is not None else None, nat.dptr(c1), nat.dptr(c2),
+                       nat.dptr(gt), Nt)
+        try:
+            if self._choose_mode() != nat.FIT_J_ELIDED:
+                raise RuntimeError("J bookkeeping: the device loop needs J = sigma*E or J = 0")
+            self._device_steps(1, Nt - 1)
+            self.nstep = n0 + Nt
+        finally:
+            self._ctx.call("fit_set_plane_source", 0, 0, 0, 0, 0, 0, None, None, None, None, 0)
+        self._after_device_run()
+
+    # ------------------------------------------------------------------ wakesolve
+    def wakesolve(self, wakelength=None, wake=None, callback=None, compute_plane="both", plot=False, plot_func=None,
+                  plot_from=None, plot_every=1, plot_until=None, save_J=False, add_space=None,
+                  use_field_monitor=False, field_monitor=None, use_edt=None, **kwargs):
+        if wake is not None:
+            self.wake = wake
+        if self.wake is None:
+            raise AttributeError("Wake solver information not passed to the solver instantiation")
+        if wakelength is None:
+            wakelength = self.wake.wakelength
+        if add_space is not None:
+            self.wake.skip_cells = add_space
+        if plot:
+            raise NotImplementedError("plotting is not provided")
+        if save_J:
+            raise NotImplementedError("save_J writes Jz.h5 every step; the beam current is evaluated in the "
+                                      "E-pass kernel and not stored")
+        wake = self.wake
+        self.xtest, self.ytest = wake.xtest, wake.ytest
+        self.ixt, self.iyt = np.abs(self.x - self.xtest).argmin(), np.abs(self.y - self.ytest).argmin()
+        longitudinal = compute_plane.lower() == "longitudinal"
+        if longitudinal:
+            xx, yy = self.ixt, self.iyt
+            lines = [(self.ixt, self.iyt)]
+        else:
+            xx, yy = slice(self.ixt - 1, self.ixt + 2), slice(self.iyt - 1, self.iyt + 2)
+            lines = [(self.ixt + i, self.iyt + j) for i in (-1, 0, 1) for j in (-1, 0, 1)]
+        wake.wakelength = wakelength
+        self.ti = wake.ti
+        self.v = wake.v
+        z = self.z
+        tmax = (wakelength + self.ti * self.v + (z.max() - z.min())) / self.v
+        Nt = int(tmax / self.dt)
+        self.tmax, self.Nt = tmax, Nt
+        beam = Beam(q=wake.q, sigmaz=wake.sigmaz, beta=wake.beta, xsource=wake.xsource, ysource=wake.ysource)
+        # what the reference writes into Ez.h5 besides the field (wakis/routines.py:403-410)
+        t = np.arange(0, Nt * self.dt, self.dt)
+        wake._attach_run(self, t=t, xf=self.x[xx], yf=self.y[yy], zf=z, dx=self.grid.dx, dy=self.grid.dy,
+                         dz=self.grid.dz, lines=lines, nsteps=Nt, longitudinal=longitudinal)
+        if self.verbose:
+            print("Running electromagnetic time-domain simulation...")
+        t0 = time.time()
+        fast = callback is None and not (use_field_monitor and field_monitor is not None)
+        if fast and Nt > 0:
+            beam._first(self)
+            self._register_beam(beam)
+            vt = np.ascontiguousarray(beam.v * _step_times(self.dt, Nt), dtype=np.float64)
+            self._ctx.call("fit_set_beam_vt_table", nat.dptr(vt), Nt)
+            n0 = self.nstep
+            first = 0
+            if self._choose_mode() != nat.FIT_J_ELIDED or self.step_0:
+                beam.update(self, 0 * self.dt)
+                self._advance(0)
+                first = 1
+            self._device_steps(first, Nt - first)
+            self.nstep = n0 + Nt
+            self._beam_vt = float(vt[-1])
+            self._beam_override = not self.use_conductivity
+            self._after_device_run()
+        else:
+            for n in range(Nt):
+                beam.update(self, n * self.dt)
+                self._advance(n)
+                if use_field_monitor and field_monitor is not None:
+                    field_monitor.update(self.E, self.dt)
+                if callback is not None:
+                    callback(self, n * self.dt)
+        self._ctx.call("fit_set_wake_taps", 0, None, None, 0, 0, 0, None, None, None, None, 0, None)
+        self.simulationTime = time.time() - t0
+        wake.solve(compute_plane=compute_plane)
+        self.logger.wakeSolver = wake.logger.wakeSolver
+        self.logger.wakeSolver["wakelength"] = wakelength
+        self.logger.wakeSolver["simulationTime"] = self.simulationTime
+        self.logger.solver["Mcell_updates_per_s"] = (self.N * Nt / self.simulationTime / 1e6
+                                                     if self.simulationTime > 0 else None)
+        self.logger.save_logs()
+
+    # ------------------------------------------------------------------ helpers
+    def _device_steps(self, n0, nsteps):
+        if nsteps <= 0:
+            return
+        if self.step_0:
+            self._set_ghosts_to_0()
+            self.step_0 = False
+        self._sync_coeffs()
+        self._ctx.call("fit_run", n0, nsteps)
+        self._run_steps += nsteps
+
+    def _after_device_run(self):
+        self._beam_armed = False
+        if self.use_conductivity:
+            self._j_state = "derived"
+            self._j_stale = True
+        self._e_zero = False
+
+    def _open_saves(self, Nt, fields, components, save_every, subdomain):
+        try:
+            import h5py
+        except ImportError:
+            h5py = None
+        hfs = {}
+        for field in fields:
+            names = [field + c for c in components] if len(field) == 1 else [field]
+            for nm in names:
+                hfs[nm] = {} if h5py is None else h5py.File(nm + ".h5", "w")
+        meta = dict(x=self.x, y=self.y, z=self.z, dx=self.grid.dx, dy=self.grid.dy, dz=self.grid.dz,
+                    t=np.arange(0, Nt * self.dt, save_every * self.dt))
+        for hf in hfs.values():
+            for k, v in meta.items():
+                hf[k] = v
+        self._save_sub = subdomain if subdomain is not None else (slice(0, self.Nx), slice(0, self.Ny),
+                                                                  slice(0, self.Nz))
+        self._save_h5 = h5py is not None
+        return hfs
+
+    def _save_step(self, hfs, n):
+        xx, yy, zz = self._save_sub
+        for name, hf in hfs.items():
+            hf["#" + str(n).zfill(5)] = getattr(self, name[0])[xx, yy, zz, name[1:]]
+
+    def _close_saves(self, hfs):
+        for name, hf in hfs.items():
+            if self._save_h5:
+                hf.close()
+            else:
+                np.savez(name + ".npz", **hf)
