@@ -176,6 +176,11 @@ FIT_API int fit_wake_finalize(FitCtx *ctx, double qscale, double ds, double dxf,
 FIT_API int fit_dft(const double *x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
             double *out);
 
+/* Benchmark support: launches the H pass reps times, then the elided-J E pass reps
+ * times (advancing the fields), on the context's stream between CUDA events; ms_out
+ * (host, 2 values) receives the average milliseconds per launch of each kernel. */
+FIT_API int fit_time_kernels(FitCtx *ctx, int32_t reps, double *ms_out);
+
 /* Library build information: sm architecture compiled for, and the kernel launch
  * counter (kernels issued since load), for bench accounting. */
 FIT_API int fit_version(char *buf, int64_t len);

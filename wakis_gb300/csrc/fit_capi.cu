@@ -848,6 +848,53 @@ int fit_dft(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, i
     return FIT_OK;
 }
 
+int fit_time_kernels(FitCtx* c, int32_t reps, double* ms_out) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (reps < 1 || !ms_out) return fail(c, FIT_ERR_ARG, "bad timing arguments");
+    rc = enter(c);
+    if (rc) return rc;
+    cudaEvent_t e0, e1, e2;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventCreate(&e2));
+    const int mode = c->use_cond ? 1 : 0;
+    StepArgs st{};
+    st.vt = c->beam_vt;
+    const int vec = pick_vec(c);
+    auto h = [&]() {
+        if (c->dtype == FIT_F64) {
+            if (vec == 2) launch_h<double, 2>(c); else launch_h<double, 1>(c);
+        } else {
+            if (vec == 4) launch_h<float, 4>(c); else if (vec == 2) launch_h<float, 2>(c); else launch_h<float, 1>(c);
+        }
+    };
+    auto e = [&]() {
+        if (c->dtype == FIT_F64) {
+            if (vec == 2) launch_e<double, 2>(c, mode, st); else launch_e<double, 1>(c, mode, st);
+        } else {
+            if (vec == 4) launch_e<float, 4>(c, mode, st);
+            else if (vec == 2) launch_e<float, 2>(c, mode, st);
+            else launch_e<float, 1>(c, mode, st);
+        }
+    };
+    CK(cudaEventRecord(e0, c->own));
+    for (int r = 0; r < reps; ++r) h();
+    CK(cudaEventRecord(e1, c->own));
+    for (int r = 0; r < reps; ++r) e();
+    CK(cudaEventRecord(e2, c->own));
+    CK(cudaEventSynchronize(e2));
+    float a = 0.f, b = 0.f;
+    CK(cudaEventElapsedTime(&a, e0, e1));
+    CK(cudaEventElapsedTime(&b, e1, e2));
+    ms_out[0] = a / reps;
+    ms_out[1] = b / reps;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    return leave(c);
+}
+
 int fit_version(char* buf, int64_t len) {
     if (!buf || len <= 0) return FIT_ERR_ARG;
     snprintf(buf, (size_t)len, "wakis_gb300 fit 0.1 sm_103a cuda %d", CUDART_VERSION);

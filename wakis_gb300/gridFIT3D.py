@@ -182,6 +182,12 @@ class GridFIT3D:
                     for c in (0, 1):
                         m |= inside[a:a + self.Nx, b:b + self.Ny, c:c + self.Nz]
             return m
+        if type(solid).__module__.startswith("torch"):
+            # a torch bool tensor (e.g. built on the GPU for large grids) stays where it is
+            if solid.numel() != self.Nx * self.Ny * self.Nz:
+                raise ValueError(f"solid mask has {solid.numel()} cells, the grid has "
+                                 f"{self.Nx * self.Ny * self.Nz}")
+            return solid.reshape(shape).bool()
         m = np.asarray(solid, dtype=bool)
         if m.size != self.Nx * self.Ny * self.Nz:
             raise ValueError(f"solid mask has {m.size} cells, the grid has {self.Nx * self.Ny * self.Nz}")

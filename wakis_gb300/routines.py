@@ -114,6 +114,36 @@ class RoutinesMixin:
             raise NotImplementedError("save_J writes Jz.h5 every step; the beam current is evaluated in the "
                                       "E-pass kernel and not stored")
         wake = self.wake
+        beam, Nt = self._wake_prepare(wake, wakelength, compute_plane)
+        if self.verbose:
+            print("Running electromagnetic time-domain simulation...")
+        t0 = time.time()
+        fast = callback is None and not (use_field_monitor and field_monitor is not None)
+        if fast and Nt > 0:
+            vt = self._wake_device_setup(beam, Nt)
+            first = self._wake_first_step(beam)
+            self._device_steps(first, Nt - first)
+            self._wake_device_done(vt, Nt)
+        else:
+            for n in range(Nt):
+                beam.update(self, n * self.dt)
+                self._advance(n)
+                if use_field_monitor and field_monitor is not None:
+                    field_monitor.update(self.E, self.dt)
+                if callback is not None:
+                    callback(self, n * self.dt)
+        self.simulationTime = time.time() - t0
+        wake.solve(compute_plane=compute_plane)
+        self.logger.wakeSolver = wake.logger.wakeSolver
+        self.logger.wakeSolver["wakelength"] = wakelength
+        self.logger.wakeSolver["simulationTime"] = self.simulationTime
+        self.logger.solver["Mcell_updates_per_s"] = (self.N * Nt / self.simulationTime / 1e6
+                                                     if self.simulationTime > 0 else None)
+        self.logger.save_logs()
+
+    # ------------------------------------------------------------------ wakesolve pieces
+    def _wake_prepare(self, wake, wakelength, compute_plane):
+        """Nt, the Beam and the device tap table of a wake run (wakis/routines.py:340-420)."""
         self.xtest, self.ytest = wake.xtest, wake.ytest
         self.ixt, self.iyt = np.abs(self.x - self.xtest).argmin(), np.abs(self.y - self.ytest).argmin()
         longitudinal = compute_plane.lower() == "longitudinal"
@@ -135,43 +165,31 @@ class RoutinesMixin:
         t = np.arange(0, Nt * self.dt, self.dt)
         wake._attach_run(self, t=t, xf=self.x[xx], yf=self.y[yy], zf=z, dx=self.grid.dx, dy=self.grid.dy,
                          dz=self.grid.dz, lines=lines, nsteps=Nt, longitudinal=longitudinal)
-        if self.verbose:
-            print("Running electromagnetic time-domain simulation...")
-        t0 = time.time()
-        fast = callback is None and not (use_field_monitor and field_monitor is not None)
-        if fast and Nt > 0:
-            beam._first(self)
-            self._register_beam(beam)
-            vt = np.ascontiguousarray(beam.v * _step_times(self.dt, Nt), dtype=np.float64)
-            self._ctx.call("fit_set_beam_vt_table", nat.dptr(vt), Nt)
-            n0 = self.nstep
-            first = 0
-            if self._choose_mode() != nat.FIT_J_ELIDED or self.step_0:
-                beam.update(self, 0 * self.dt)
-                self._advance(0)
-                first = 1
-            self._device_steps(first, Nt - first)
-            self.nstep = n0 + Nt
-            self._beam_vt = float(vt[-1])
-            self._beam_override = not self.use_conductivity
-            self._after_device_run()
-        else:
-            for n in range(Nt):
-                beam.update(self, n * self.dt)
-                self._advance(n)
-                if use_field_monitor and field_monitor is not None:
-                    field_monitor.update(self.E, self.dt)
-                if callback is not None:
-                    callback(self, n * self.dt)
-        self._ctx.call("fit_set_wake_taps", 0, None, None, 0, 0, 0, None, None, None, None, 0, None)
-        self.simulationTime = time.time() - t0
-        wake.solve(compute_plane=compute_plane)
-        self.logger.wakeSolver = wake.logger.wakeSolver
-        self.logger.wakeSolver["wakelength"] = wakelength
-        self.logger.wakeSolver["simulationTime"] = self.simulationTime
-        self.logger.solver["Mcell_updates_per_s"] = (self.N * Nt / self.simulationTime / 1e6
-                                                     if self.simulationTime > 0 else None)
-        self.logger.save_logs()
+        return beam, Nt
+
+    def _wake_device_setup(self, beam, Nt):
+        """Beam and its v*t table on the device for graph-replayed steps 0..Nt-1."""
+        beam._first(self)
+        self._register_beam(beam)
+        vt = np.ascontiguousarray(beam.v * _step_times(self.dt, Nt), dtype=np.float64)
+        self._ctx.call("fit_set_beam_vt_table", nat.dptr(vt), Nt)
+        self._wake_n0 = self.nstep
+        return vt
+
+    def _wake_first_step(self, beam):
+        """Takes step 0 from the host when the device loop cannot (first step: ghost
+        zeroing; J not equal to what the loss factor assumes).  Returns the next step."""
+        if self._choose_mode() != nat.FIT_J_ELIDED or self.step_0:
+            beam.update(self, 0 * self.dt)
+            self._advance(0)
+            return 1
+        return 0
+
+    def _wake_device_done(self, vt, Nt):
+        self.nstep = self._wake_n0 + Nt
+        self._beam_vt = float(vt[-1])
+        self._beam_override = not self.use_conductivity
+        self._after_device_run()
 
     # ------------------------------------------------------------------ helpers
     def _device_steps(self, n0, nsteps):

@@ -133,16 +133,6 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._dt = dt
         self.update_logger(["dt"])
 
-        # native context
-        self._ctx = nat.Context(self.Nx, self.Ny, self.Nz, self.dtype, self.use_conductivity, self.bc_low,
-                                self.bc_high, self.E.array, self.H.array, self._J.array, device=dev.index)
-        self._ctx.call("fit_set_stream", nat.C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
-        self._metric_arrays = [np.ascontiguousarray(a, dtype=np.float64)
-                               for a in (grid.dx, grid.dy, grid.dz, grid.tdx, grid.tdy, grid.tdz)]
-        self._ctx.call("fit_set_metrics", *[nat.dptr(a) for a in self._metric_arrays])
-        self._coeff_dt = None
-        self._sync_coeffs()
-
         # J bookkeeping: 'tensor' = the J storage is the truth; 'derived' = the truth is
         # sigma*E (tensor refreshed on read).  _j_zero: storage known to be zero except the
         # beam line; _e_zero: E known to be zero.
@@ -155,6 +145,17 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._beam_armed = False
         self._beam_override = False
         self._explicit_ready = False
+
+        # native context
+        self._ctx = nat.Context(self.Nx, self.Ny, self.Nz, self.dtype, self.use_conductivity, self.bc_low,
+                                self.bc_high, self.E.array, self.H.array, self._J.array, device=dev.index)
+        self._ctx.call("fit_set_stream", nat.C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+        self._metric_arrays = [np.ascontiguousarray(a, dtype=np.float64)
+                               for a in (grid.dx, grid.dy, grid.dz, grid.tdx, grid.tdy, grid.tdz)]
+        self._ctx.call("fit_set_metrics", *[nat.dptr(a) for a in self._metric_arrays])
+        self._coeff_dt = None
+        self._sync_coeffs()
+
         self.E._on_write = self._before_E_write
         self._J._on_write = self._before_J_write
         self.one_step = self._one_step
@@ -208,9 +209,14 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
 
     # ------------------------------------------------------------------ materials
     def _mask_gpu(self, key):
-        m = np.asarray(self.grid.grid[key]).astype(bool).reshape(self.Nx, self.Ny, self.Nz)
-        t = torch.as_tensor(np.ascontiguousarray(m.transpose(2, 1, 0)).reshape(-1), device=self.device)
-        return t.repeat(3)
+        """grid.grid[key] (C order over (Nx, Ny, Nz), as wakis/solverFIT3D.py:462 reshapes
+        it) -> a 3N bool tensor in the Field layout (Fortran order, all 3 components)."""
+        src = self.grid.grid[key]
+        if isinstance(src, torch.Tensor):
+            m = src.to(self.device).bool().reshape(self.Nx, self.Ny, self.Nz)
+        else:
+            m = torch.as_tensor(np.asarray(src).astype(bool).reshape(self.Nx, self.Ny, self.Nz), device=self.device)
+        return m.permute(2, 1, 0).contiguous().reshape(-1).repeat(3)
 
     def _apply_stl_materials(self):
         """Solid masks -> ieps, imu, sigma (wakis/solverFIT3D.py:438-502)."""
