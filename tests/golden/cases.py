@@ -194,7 +194,7 @@ def random_fields(N, seed, dtype):
 def probe_points(c):
     """Seeded interior probe cells (outside the PML) for the emsolve cases."""
     x, y, z = axes(c)
-    n = c.get("n_pml", 0)
+    n = c.get("probe_margin", c.get("n_pml", 0))
     rng = np.random.default_rng(2)
     Nx, Ny, Nz = len(x) - 1, len(y) - 1, len(z) - 1
     return np.stack([rng.integers(n, Nx - n, c["probes"]), rng.integers(n, Ny - n, c["probes"]),

@@ -431,7 +431,11 @@ __global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __res
         ldg_v<T, VEC>(ax, cj + n);
         ldg_v<T, VEC>(ay, cj + g.N + n);
         ldg_v<T, VEC>(az, cj + 2 * g.N + n);
-        if (on_line) jz[b.ixs - i0] = (T)jb;
+        if (on_line) {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e)
+                if (i0 + e == b.ixs) jz[e] = (T)jb;
+        }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
             ex[e] = ex[e] + kx[e] * cur[0][e] - ax[e] * jx[e];
@@ -458,9 +462,11 @@ __global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __res
     }
     if constexpr (MODE != 2) {
         if (on_line) {
-            const int e = b.ixs - i0;
-            ez[e] = ez[e] - (T)b.dtieps[k] * (T)jb;
-            if (!use_cond) J[2 * g.N + n + e] = (T)jb;  // J keeps the last beam value
+            const T dj = (T)b.dtieps[k] * (T)jb;
+#pragma unroll
+            for (int e = 0; e < VEC; ++e)
+                if (i0 + e == b.ixs) ez[e] = ez[e] - dj;
+            if (!use_cond) J[2 * g.N + n + (b.ixs - i0)] = (T)jb;  // J keeps the last beam value
         }
     }
     st_v<T, VEC>(E + n, ex);

@@ -241,4 +241,10 @@ class GridFIT3D:
 
     def update_logger(self, attrs):
         for atr in attrs:
-            self.logger.grid[atr] = getattr(self, atr)
+            val = getattr(self, atr)
+            if atr == "stl_solids" and isinstance(val, dict):
+                # solids are masks or callables here, not file names: log what they are
+                val = {k: (v if isinstance(v, str) else
+                           f"mask{tuple(v.shape)}" if hasattr(v, "shape") else getattr(v, "__name__", type(v).__name__))
+                       for k, v in val.items()}
+            self.logger.grid[atr] = val

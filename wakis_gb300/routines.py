@@ -41,8 +41,12 @@ class RoutinesMixin:
             hfs = self._open_saves(Nt, fields, components, save_every, subdomain)
         abc_axes = self._abc_lo_axes() if self.activate_abc else 0
         self._ctx.call("fit_set_abc", abc_axes)
+        # J = sigma*E is taken at the end of the step, before the ABC copy changes plane 0,
+        # so on a conductive grid J stays explicit while ABC faces are updated
+        self._force_explicit = bool(abc_axes) and self.use_conductivity
         try:
-            fast = (callback is None and not save and type(source) in (PlaneWave, WavePacket))
+            fast = (callback is None and not save and type(source) in (PlaneWave, WavePacket)
+                    and not self._force_explicit)
             if fast and Nt > 0:
                 self._emsolve_device(Nt, source)
             else:
@@ -56,6 +60,10 @@ class RoutinesMixin:
                         callback(self, n * self.dt)
         finally:
             self._ctx.call("fit_set_abc", 0)
+            if self._force_explicit:
+                # J holds sigma*E of the pre-ABC planes: it stays the truth for the next step
+                self._j_state, self._j_zero, self._j_stale = "tensor", False, False
+            self._force_explicit = False
             if hfs is not None:
                 self._close_saves(hfs)
 

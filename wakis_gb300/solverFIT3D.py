@@ -145,6 +145,7 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._beam_armed = False
         self._beam_override = False
         self._explicit_ready = False
+        self._force_explicit = False  # emsolve with ABC faces on a conductive grid
 
         # native context
         self._ctx = nat.Context(self.Nx, self.Ny, self.Nz, self.dtype, self.use_conductivity, self.bc_low,
@@ -176,17 +177,16 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
 
     def _tau_min(self):
         """min over sigma != 0 and ieps != 0 of (1/ieps)/sigma, in the solver dtype
-        (wakis/solverFIT3D.py:309-318); the (ieps, sigma) pairs are few, so they are
-        reduced on the device and the quotient is evaluated on the host in numpy."""
+        (wakis/solverFIT3D.py:309-318).  Evaluated on the device with IEEE division in the
+        solver dtype (the values are those numpy computes on the host)."""
         ie, sg = self.ieps.array, self.sigma.array
         if self.dtype == np.float32:
             ie, sg = ie.float(), sg.float()
         mask = (sg != 0) & (ie != 0)
-        pairs = torch.unique(torch.stack([ie[mask], sg[mask]], dim=1), dim=0).cpu().numpy()
-        if pairs.shape[0] == 0:
+        if not bool(mask.any()):
             raise ValueError("zero-size array to reduction operation minimum which has no identity")
-        tau = (1 / pairs[:, 0].astype(self.dtype)) / pairs[:, 1].astype(self.dtype)
-        return tau.min()
+        tau = torch.where(mask, (1 / ie) / sg, torch.full((), float("inf"), dtype=ie.dtype, device=ie.device))
+        return self.dtype(tau.min().item())
 
     def _sync_coeffs(self):
         dt = float(self._dt)
@@ -308,6 +308,8 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
 
     def _choose_mode(self):
         """FIT_J_ELIDED when J is what the loss factor assumes, else FIT_J_EXPLICIT."""
+        if self._force_explicit:
+            return nat.FIT_J_EXPLICIT
         if self.use_conductivity:
             if self._j_state == "derived" or (self._j_zero and self._e_zero):
                 return nat.FIT_J_ELIDED
