@@ -176,6 +176,15 @@ FIT_API int fit_wake_finalize(FitCtx *ctx, double qscale, double ds, double dxf,
 FIT_API int fit_dft(const double *x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
             double *out);
 
+/* Reads the context's device error word (synchronizes the context stream): FIT_OK, or
+ * FIT_ERR_TIMEOUT when a kernel gave up a bounded wait on its bulk copies (the kernel
+ * then returned without completing its pass).  The word is cleared by the read. */
+FIT_API int fit_check_error(FitCtx *ctx);
+
+/* Chooses the pass kernels: staged != 0 (default) uses the persistent bulk-copy kernels
+ * when Nx*sizeof(dtype) is a multiple of 16 bytes; 0 always uses the direct kernels. */
+FIT_API int fit_set_kernel_variant(FitCtx *ctx, int32_t staged);
+
 /* Benchmark support: launches the H pass reps times, then the elided-J E pass reps
  * times (advancing the fields), on the context's stream between CUDA events; ms_out
  * (host, 2 values) receives the average milliseconds per launch of each kernel. */

@@ -91,6 +91,25 @@ def test_planewave_step_loop_matches_device_loop(tmp_path):
         assert _err(got[k], ref[k]) <= 1e-3, k
 
 
+@pytest.mark.parametrize("name", ["lossy_f32", "cavity_f64", "mixed_bc_f64", "pmc_beam_f64"])
+def test_staged_kernels_match_direct_kernels(name, tmp_path, monkeypatch):
+    """The persistent bulk-copy kernels and the direct-load kernels run the same
+    arithmetic: fields and wakes agree bit for bit."""
+    import wakis_gb300.solverFIT3D as sf
+    orig = sf.SolverFIT3D._sync_coeffs
+    out = []
+    for staged in (1, 0):
+        def patched(self, _o=orig, _s=staged):
+            self._ctx.call("fit_set_kernel_variant", _s)
+            _o(self)
+        monkeypatch.setattr(sf.SolverFIT3D, "_sync_coeffs", patched)
+        out.append(run_case(name, tmpdir=tmp_path))
+    monkeypatch.setattr(sf.SolverFIT3D, "_sync_coeffs", orig)
+    for k in ("E", "H", "J", "WP", "Z"):
+        if k in out[0]:
+            np.testing.assert_array_equal(out[0][k], out[1][k], err_msg=k)
+
+
 def test_wake_step_loop_matches_device_loop(tmp_path):
     """wakesolve with a callback (Python step loop) equals the graph-replayed loop."""
     import wakis_gb300 as wg

@@ -81,6 +81,9 @@ struct FitCtx {
     cudaGraphExec_t graph = nullptr;
     long long graph_chunk = 0;
     bool capturing = false;
+    int* d_err = nullptr;   // device error word written by kernels (FIT_ERR_TIMEOUT)
+    int nsm = 1;            // SM count: grid of the persistent staged kernels
+    bool staged = true;     // staged (bulk-copy) passes when the grid is aligned
     std::string err;
 };
 
@@ -187,18 +190,39 @@ int launches_per_step(const FitCtx* c) {
     return n;
 }
 
+// staged kernels need 16-byte aligned stream starts: Nx*sizeof(T) % 16 == 0
+bool staged_ok(const FitCtx* c) { return c->staged && ((long long)c->g.nx * (long long)esize(c)) % 16 == 0; }
+
+constexpr int kNstH = 4, kNstE = 3;
+
+template <typename T, int VEC, int NS, int NST>
+size_t staged_bytes() {
+    return (size_t)NST * ((size_t)NS * 256 * VEC + 2 * (16 / sizeof(T))) * sizeof(T) + NST * sizeof(unsigned long long);
+}
+
+template <typename KernelPtr>
+void allow_smem(KernelPtr k, size_t bytes) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 template <typename T, int VEC>
 void launch_h(FitCtx* c) {
-    const long long nv = c->g.N / VEC;
-    k_hpass<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
-                                                         static_cast<const T*>(c->ch), c->g, metric<T>(c));
+    if (VEC * sizeof(T) == 16 && staged_ok(c)) {
+        const size_t sm = staged_bytes<T, VEC, 13, kNstH>();
+        auto k = k_hpass_staged<T, VEC, kNstH>;
+        allow_smem(k, sm);
+        k<<<c->nsm, 256, sm, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
+                                       static_cast<const T*>(c->ch), c->g, metric<T>(c), c->d_err);
+    } else {
+        const long long nv = c->g.N / VEC;
+        k_hpass<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
+                                                             static_cast<const T*>(c->ch), c->g, metric<T>(c));
+    }
     count(c);
 }
 
 template <typename T, int VEC>
 void launch_e(FitCtx* c, int mode, const StepArgs& st) {
-    const long long nv = c->g.N / VEC;
-    const unsigned nb = grid1d(nv, 256);
     T* E = static_cast<T*>(c->E);
     const T* H = static_cast<const T*>(c->H);
     const T* ce = static_cast<const T*>(c->ce);
@@ -206,6 +230,25 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
     T* J = static_cast<T*>(c->J);
     const T* cj = static_cast<const T*>(c->cj);
     const T* sg = static_cast<const T*>(c->sg);
+    if (VEC * sizeof(T) == 16 && staged_ok(c) && mode != 2) {
+        if (mode == 1) {
+            const size_t sm = staged_bytes<T, VEC, 16, kNstE>();
+            auto k = k_epass_staged<T, VEC, kNstE, 1>;
+            allow_smem(k, sm);
+            k<<<c->nsm, 256, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
+                                           c->d_err);
+        } else {
+            const size_t sm = staged_bytes<T, VEC, 13, kNstE>();
+            auto k = k_epass_staged<T, VEC, kNstE, 0>;
+            allow_smem(k, sm);
+            k<<<c->nsm, 256, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
+                                           c->d_err);
+        }
+        count(c);
+        return;
+    }
+    const long long nv = c->g.N / VEC;
+    const unsigned nb = grid1d(nv, 256);
     if (mode == 0)
         k_epass<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
     else if (mode == 1)
@@ -335,6 +378,9 @@ int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_step, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) {
         int rc = fail(nullptr, FIT_ERR_CUDA, "context setup failed: %s", cudaGetErrorString(e));
         fit_ctx_destroy(c);
@@ -369,7 +415,7 @@ int fit_ctx_destroy(FitCtx* c) {
                     (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
                     (void*)c->d_em, (void*)c->d_ek0, (void*)c->d_ecnt, (void*)c->d_dz, (void*)c->d_acc,
                     (void*)c->d_comp, (void*)c->d_scratch, (void*)c->d_wp3d, (void*)c->d_wpx, (void*)c->d_wpy,
-                    (void*)c->d_step})
+                    (void*)c->d_step, (void*)c->d_err})
         dfree(p);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
@@ -893,6 +939,30 @@ int fit_time_kernels(FitCtx* c, int32_t reps, double* ms_out) {
     cudaEventDestroy(e1);
     cudaEventDestroy(e2);
     return leave(c);
+}
+
+int fit_check_error(FitCtx* c) {
+    if (!c) return FIT_ERR_ARG;
+    int rc = enter(c);
+    if (rc) return rc;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->own));
+    CK(cudaStreamSynchronize(c->own));
+    rc = leave(c);
+    if (rc) return rc;
+    if (h != 0) {
+        int z = 0;
+        cudaMemcpy(c->d_err, &z, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(c, h, "a kernel gave up waiting for its bulk copies (error %d)", h);
+    }
+    return FIT_OK;
+}
+
+int fit_set_kernel_variant(FitCtx* c, int32_t staged) {
+    if (!c) return FIT_ERR_ARG;
+    invalidate(c);
+    c->staged = staged != 0;
+    return FIT_OK;
 }
 
 int fit_version(char* buf, int64_t len) {

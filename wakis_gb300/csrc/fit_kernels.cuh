@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "wakis_fit.h"
+
 namespace fit {
 
 // face bit f: 0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi, 4 z-lo, 5 z-hi
@@ -215,62 +217,22 @@ struct PlaneArgs {
     double* stash;  // E_x of the plane before the source overwrote it (loss term)
 };
 
-// ---------------------------------------------------------------- H pass
-// H_c <- H_c - ch_c * (C ê)_c, one thread per VEC consecutive x cells.
+// ---------------------------------------------------------------- pass arithmetic
+// One thread updates VEC consecutive x cells (i0..i0+VEC-1, j, k).  The inputs are the
+// VEC values of each stream at the thread's cells (own, +Nx row, +Nx*Ny plane) and the
+// one value just past the vector along x; they come from registers (direct kernels)
+// or from shared memory (staged kernels).
+
+// H_c <- H_c - ch_c * (C ê)_c
 template <typename T, int VEC>
-__global__ void __launch_bounds__(256) k_hpass(const T* __restrict__ E, T* __restrict__ H,
-                                               const T* __restrict__ ch, Geom g, Metric<T> mt) {
-    const long long nvec = g.N / VEC;
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nvec) return;
-    const long long n = v * VEC;
-    const int i0 = (int)(n % g.nx);
-    const long long r = n / g.nx;
-    const int j = (int)(r % g.ny);
-    const int k = (int)(r / g.ny);
-    const T* Ex = E;
-    const T* Ey = E + g.N;
-    const T* Ez = E + 2 * g.N;
-
-    T ex[VEC], ey[VEC], ez[VEC];
-    ldg_v<T, VEC>(ex, Ex + n);
-    ldg_v<T, VEC>(ey, Ey + n);
-    ldg_v<T, VEC>(ez, Ez + n);
-    // y-forward row (n + Nx) and z-forward plane (n + Nx*Ny)
-    const bool yv = (j + 1 < g.ny) || (k + 1 < g.nz);
-    const bool zv = (k + 1 < g.nz);
-    T exy[VEC], ezy[VEC], exz[VEC], eyz[VEC];
-    if (yv) {
-        ldg_v<T, VEC>(exy, Ex + n + g.sy);
-        ldg_v<T, VEC>(ezy, Ez + n + g.sy);
-    } else {
-        zero_v<T, VEC>(exy);
-        zero_v<T, VEC>(ezy);
-    }
-    if (zv) {
-        ldg_v<T, VEC>(exz, Ex + n + g.sz);
-        ldg_v<T, VEC>(eyz, Ey + n + g.sz);
-    } else {
-        zero_v<T, VEC>(exz);
-        zero_v<T, VEC>(eyz);
-    }
-    // x-forward of the last element
+__device__ __forceinline__ void hpass_cells(const T (&ex)[VEC], const T (&ey)[VEC], const T (&ez)[VEC],
+                                            const T (&exy)[VEC], const T (&ezy)[VEC], const T (&exz)[VEC],
+                                            const T (&eyz)[VEC], T eyx, T ezx, T (&hx)[VEC], T (&hy)[VEC],
+                                            T (&hz)[VEC], const T (&cx)[VEC], const T (&cy)[VEC],
+                                            const T (&cz)[VEC], int i0, int j, int k, const Geom& g,
+                                            const Metric<T>& mt) {
     const Nb xl = fwd_x(i0 + VEC - 1, j, k, g);
-    T eyx = T(0), ezx = T(0);
-    if (xl.valid) {
-        eyx = __ldg(Ey + n + VEC);
-        ezx = __ldg(Ez + n + VEC);
-    }
-
-    T hx[VEC], hy[VEC], hz[VEC], cx[VEC], cy[VEC], cz[VEC];
-    ld_v<T, VEC>(hx, H + n);
-    ld_v<T, VEC>(hy, H + g.N + n);
-    ld_v<T, VEC>(hz, H + 2 * g.N + n);
-    ldg_v<T, VEC>(cx, ch + n);
-    ldg_v<T, VEC>(cy, ch + g.N + n);
-    ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
-
-    const Nb py = fwd_y(i0, j, k, g);  // i replaced per element below
+    const Nb py = fwd_y(i0, j, k, g);
     const Nb pz = fwd_z(i0, j, k, g);
 #pragma unroll
     for (int e = 0; e < VEC; ++e) {
@@ -296,12 +258,152 @@ __global__ void __launch_bounds__(256) k_hpass(const T* __restrict__ E, T* __res
         hy[e] = hy[e] - cy[e] * curly;
         hz[e] = hz[e] - cz[e] * curlz;
     }
+}
+
+// (C^T ĥ)_c of VEC cells, D^T_a v[m] = v[m - s_a] - v[m]
+template <typename T, int VEC>
+__device__ __forceinline__ void epass_curl(const T (&hx)[VEC], const T (&hy)[VEC], const T (&hz)[VEC],
+                                           const T (&hxy)[VEC], const T (&hzy)[VEC], const T (&hxz)[VEC],
+                                           const T (&hyz)[VEC], T hyx, T hzx, T (&cur)[3][VEC], int i0, int j,
+                                           int k, const Geom& g, const Metric<T>& mt) {
+    const Nb xf = bwd_x(i0, j, k, g);
+    const Nb py = bwd_y(i0, j, k, g);
+    const Nb pz = bwd_z(i0, j, k, g);
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+        const int i = i0 + e;
+        const Nb p0{i, j, k, true};
+        const Nb pyi{i, py.j, py.k, py.valid};
+        const Nb pzi{i, pz.j, pz.k, pz.valid};
+        const Nb pxi = (e > 0) ? Nb{i - 1, j, k, true} : xf;
+        const T hx0 = hhat<T>(hx[e], 0, p0, g, mt);
+        const T hy0 = hhat<T>(hy[e], 1, p0, g, mt);
+        const T hz0 = hhat<T>(hz[e], 2, p0, g, mt);
+        const T hxY = hhat<T>(hxy[e], 0, pyi, g, mt);
+        const T hzY = hhat<T>(hzy[e], 2, pyi, g, mt);
+        const T hxZ = hhat<T>(hxz[e], 0, pzi, g, mt);
+        const T hyZ = hhat<T>(hyz[e], 1, pzi, g, mt);
+        const T hyX = hhat<T>((e > 0) ? hy[e - 1] : hyx, 1, pxi, g, mt);
+        const T hzX = hhat<T>((e > 0) ? hz[e - 1] : hzx, 2, pxi, g, mt);
+        // (C^T ĥ)_x = D^T_z ĥ_y - D^T_y ĥ_z ; (C^T ĥ)_y = -D^T_z ĥ_x + D^T_x ĥ_z ;
+        // (C^T ĥ)_z = D^T_y ĥ_x - D^T_x ĥ_y
+        cur[0][e] = (hyZ - hy0) + (hz0 - hzY);
+        cur[1][e] = (hx0 - hxZ) + (hzX - hz0);
+        cur[2][e] = (hxY - hx0) + (hy0 - hyX);
+    }
+}
+
+// Elided-J E update of VEC cells (MODE 0: no conduction current, MODE 1: loss factor),
+// with the beam line current and the hard-source plane (stash) corrections.
+template <typename T, int VEC, int MODE>
+__device__ __forceinline__ void epass_update(T (&ex)[VEC], T (&ey)[VEC], T (&ez)[VEC], const T (&kx)[VEC],
+                                             const T (&ky)[VEC], const T (&kz)[VEC], const T (&lx)[VEC],
+                                             const T (&ly)[VEC], const T (&lz)[VEC], const T (&cur)[3][VEC],
+                                             T* __restrict__ J, long long n, int i0, int j, int k, int use_cond,
+                                             const Geom& g, const BeamArgs& b, const PlaneArgs& pl,
+                                             const StepArgs& st) {
+    const bool on_line = b.active && (j == b.iys) && (b.ixs >= i0) && (b.ixs < i0 + VEC);
+    double jb = 0.0;
+    if (on_line) {
+        long long sn;
+        double vt;
+        resolve_step(st, sn, vt);
+        jb = beam_current(b, k, vt);
+    }
+    if constexpr (MODE == 0) {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            ex[e] = ex[e] + kx[e] * cur[0][e];
+            ey[e] = ey[e] + ky[e] * cur[1][e];
+            ez[e] = ez[e] + kz[e] * cur[2][e];
+        }
+    } else {
+        // on the hard-source plane the conduction current is sigma times the E_x the
+        // source overwrote (J was computed at the end of the previous step)
+        const bool on_plane = pl.active && k == pl.zs && j >= pl.y0 && j < pl.y1;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int i = i0 + e;
+            if (on_plane && i >= pl.x0 && i < pl.x1)
+                ex[e] = (ex[e] - (T(1) - lx[e]) * (T)pl.stash[(i - pl.x0) + (j - pl.y0) * (pl.x1 - pl.x0)]) +
+                        kx[e] * cur[0][e];
+            else
+                ex[e] = lx[e] * ex[e] + kx[e] * cur[0][e];
+            ey[e] = ly[e] * ey[e] + ky[e] * cur[1][e];
+            // on the beam line J was overwritten by the beam: no sigma*E term there
+            ez[e] = ((on_line && (i0 + e == b.ixs)) ? ez[e] : lz[e] * ez[e]) + kz[e] * cur[2][e];
+        }
+    }
+    if (on_line) {
+        const T dj = (T)b.dtieps[k] * (T)jb;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e)
+            if (i0 + e == b.ixs) ez[e] = ez[e] - dj;
+        if (!use_cond) J[2 * g.N + n + (b.ixs - i0)] = (T)jb;  // J keeps the last beam value
+    }
+}
+
+__device__ __forceinline__ void cell_of(long long n, const Geom& g, int& i0, int& j, int& k) {
+    i0 = (int)(n % g.nx);
+    const long long r = n / g.nx;
+    j = (int)(r % g.ny);
+    k = (int)(r / g.ny);
+}
+
+// ---------------------------------------------------------------- direct kernels
+// One thread per VEC cells, inputs loaded straight from global memory.  Used for grids
+// whose Nx is not a multiple of the 16-byte vector width and for the explicit-J pass.
+template <typename T, int VEC>
+__global__ void __launch_bounds__(256) k_hpass(const T* __restrict__ E, T* __restrict__ H,
+                                               const T* __restrict__ ch, Geom g, Metric<T> mt) {
+    const long long nvec = g.N / VEC;
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvec) return;
+    const long long n = v * VEC;
+    int i0, j, k;
+    cell_of(n, g, i0, j, k);
+    const T* Ex = E;
+    const T* Ey = E + g.N;
+    const T* Ez = E + 2 * g.N;
+    T ex[VEC], ey[VEC], ez[VEC];
+    ldg_v<T, VEC>(ex, Ex + n);
+    ldg_v<T, VEC>(ey, Ey + n);
+    ldg_v<T, VEC>(ez, Ez + n);
+    const bool yv = (j + 1 < g.ny) || (k + 1 < g.nz);
+    const bool zv = (k + 1 < g.nz);
+    T exy[VEC], ezy[VEC], exz[VEC], eyz[VEC];
+    if (yv) {
+        ldg_v<T, VEC>(exy, Ex + n + g.sy);
+        ldg_v<T, VEC>(ezy, Ez + n + g.sy);
+    } else {
+        zero_v<T, VEC>(exy);
+        zero_v<T, VEC>(ezy);
+    }
+    if (zv) {
+        ldg_v<T, VEC>(exz, Ex + n + g.sz);
+        ldg_v<T, VEC>(eyz, Ey + n + g.sz);
+    } else {
+        zero_v<T, VEC>(exz);
+        zero_v<T, VEC>(eyz);
+    }
+    T eyx = T(0), ezx = T(0);
+    if (n + VEC < g.N) {
+        eyx = __ldg(Ey + n + VEC);
+        ezx = __ldg(Ez + n + VEC);
+    }
+    T hx[VEC], hy[VEC], hz[VEC], cx[VEC], cy[VEC], cz[VEC];
+    ld_v<T, VEC>(hx, H + n);
+    ld_v<T, VEC>(hy, H + g.N + n);
+    ld_v<T, VEC>(hz, H + 2 * g.N + n);
+    ldg_v<T, VEC>(cx, ch + n);
+    ldg_v<T, VEC>(cy, ch + g.N + n);
+    ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
+    hpass_cells<T, VEC>(ex, ey, ez, exy, ezy, exz, eyz, eyx, ezx, hx, hy, hz, cx, cy, cz, i0, j, k, g, mt);
     st_v<T, VEC>(H + n, hx);
     st_v<T, VEC>(H + g.N + n, hy);
     st_v<T, VEC>(H + 2 * g.N + n, hz);
 }
 
-// ---------------------------------------------------------------- E pass
 // MODE 0: E += ce*(C^T ĥ)                       (no conduction current)
 // MODE 1: E = cl*E + ce*(C^T ĥ)                 (J = sigma*E_prev folded into cl)
 // MODE 2: E = E + ce*(C^T ĥ) - cj*J; J = sg*E   (explicit J; J written if conductive)
@@ -316,14 +418,11 @@ __global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __res
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvec) return;
     const long long n = v * VEC;
-    const int i0 = (int)(n % g.nx);
-    const long long r = n / g.nx;
-    const int j = (int)(r % g.ny);
-    const int k = (int)(r / g.ny);
+    int i0, j, k;
+    cell_of(n, g, i0, j, k);
     const T* Hx = H;
     const T* Hy = H + g.N;
     const T* Hz = H + 2 * g.N;
-
     T hx[VEC], hy[VEC], hz[VEC];
     ldg_v<T, VEC>(hx, Hx + n);
     ldg_v<T, VEC>(hy, Hy + n);
@@ -345,13 +444,13 @@ __global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __res
         zero_v<T, VEC>(hxz);
         zero_v<T, VEC>(hyz);
     }
-    const Nb xf = bwd_x(i0, j, k, g);
     T hyx = T(0), hzx = T(0);
-    if (xf.valid) {
+    if (n > 0) {
         hyx = __ldg(Hy + n - 1);
         hzx = __ldg(Hz + n - 1);
     }
-
+    T cur[3][VEC];
+    epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
     T ex[VEC], ey[VEC], ez[VEC], kx[VEC], ky[VEC], kz[VEC];
     ld_v<T, VEC>(ex, E + n);
     ld_v<T, VEC>(ey, E + g.N + n);
@@ -359,71 +458,15 @@ __global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __res
     ldg_v<T, VEC>(kx, ce + n);
     ldg_v<T, VEC>(ky, ce + g.N + n);
     ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
-
-    const Nb py = bwd_y(i0, j, k, g);
-    const Nb pz = bwd_z(i0, j, k, g);
-    T cur[3][VEC];
-#pragma unroll
-    for (int e = 0; e < VEC; ++e) {
-        const int i = i0 + e;
-        const Nb p0{i, j, k, true};
-        const Nb pyi{i, py.j, py.k, py.valid};
-        const Nb pzi{i, pz.j, pz.k, pz.valid};
-        const Nb pxi = (e > 0) ? Nb{i - 1, j, k, true} : xf;
-        const T hx0 = hhat<T>(hx[e], 0, p0, g, mt);
-        const T hy0 = hhat<T>(hy[e], 1, p0, g, mt);
-        const T hz0 = hhat<T>(hz[e], 2, p0, g, mt);
-        const T hxY = hhat<T>(hxy[e], 0, pyi, g, mt);
-        const T hzY = hhat<T>(hzy[e], 2, pyi, g, mt);
-        const T hxZ = hhat<T>(hxz[e], 0, pzi, g, mt);
-        const T hyZ = hhat<T>(hyz[e], 1, pzi, g, mt);
-        const T hyX = hhat<T>((e > 0) ? hy[e - 1] : hyx, 1, pxi, g, mt);
-        const T hzX = hhat<T>((e > 0) ? hz[e - 1] : hzx, 2, pxi, g, mt);
-        // (C^T ĥ)_x = D^T_z ĥ_y - D^T_y ĥ_z ; (C^T ĥ)_y = -D^T_z ĥ_x + D^T_x ĥ_z ;
-        // (C^T ĥ)_z = D^T_y ĥ_x - D^T_x ĥ_y   with D^T_a v[m] = v[m - s_a] - v[m]
-        cur[0][e] = (hyZ - hy0) + (hz0 - hzY);
-        cur[1][e] = (hx0 - hxZ) + (hzX - hz0);
-        cur[2][e] = (hxY - hx0) + (hy0 - hyX);
-    }
-
-    // beam line of the z component
-    const bool on_line = b.active && (j == b.iys) && (b.ixs >= i0) && (b.ixs < i0 + VEC);
-    double jb = 0.0;
-    if (on_line) {
-        long long sn;
-        double vt;
-        resolve_step(st, sn, vt);
-        jb = beam_current(b, k, vt);
-    }
-
-    if constexpr (MODE == 0) {
-#pragma unroll
-        for (int e = 0; e < VEC; ++e) {
-            ex[e] = ex[e] + kx[e] * cur[0][e];
-            ey[e] = ey[e] + ky[e] * cur[1][e];
-            ez[e] = ez[e] + kz[e] * cur[2][e];
+    if constexpr (MODE == 2) {
+        const bool on_line = b.active && (j == b.iys) && (b.ixs >= i0) && (b.ixs < i0 + VEC);
+        double jb = 0.0;
+        if (on_line) {
+            long long sn;
+            double vt;
+            resolve_step(st, sn, vt);
+            jb = beam_current(b, k, vt);
         }
-    } else if constexpr (MODE == 1) {
-        T lx[VEC], ly[VEC], lz[VEC];
-        ldg_v<T, VEC>(lx, cl + n);
-        ldg_v<T, VEC>(ly, cl + g.N + n);
-        ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
-        // on the hard-source plane the conduction current is sigma times the E_x the
-        // source overwrote (J was computed at the end of the previous step)
-        const bool on_plane = pl.active && k == pl.zs && j >= pl.y0 && j < pl.y1;
-#pragma unroll
-        for (int e = 0; e < VEC; ++e) {
-            const int i = i0 + e;
-            if (on_plane && i >= pl.x0 && i < pl.x1)
-                ex[e] = (ex[e] - (T(1) - lx[e]) * (T)pl.stash[(i - pl.x0) + (j - pl.y0) * (pl.x1 - pl.x0)]) +
-                        kx[e] * cur[0][e];
-            else
-                ex[e] = lx[e] * ex[e] + kx[e] * cur[0][e];
-            ey[e] = ly[e] * ey[e] + ky[e] * cur[1][e];
-            // on the beam line J was overwritten by the beam: no sigma*E term there
-            ez[e] = ((on_line && (i0 + e == b.ixs)) ? ez[e] : lz[e] * ez[e]) + kz[e] * cur[2][e];
-        }
-    } else {
         T jx[VEC], jy[VEC], jz[VEC], ax[VEC], ay[VEC], az[VEC];
         ld_v<T, VEC>(jx, J + n);
         ld_v<T, VEC>(jy, J + g.N + n);
@@ -459,19 +502,324 @@ __global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __res
         } else if (on_line) {
             J[2 * g.N + n + (b.ixs - i0)] = (T)jb;
         }
-    }
-    if constexpr (MODE != 2) {
-        if (on_line) {
-            const T dj = (T)b.dtieps[k] * (T)jb;
-#pragma unroll
-            for (int e = 0; e < VEC; ++e)
-                if (i0 + e == b.ixs) ez[e] = ez[e] - dj;
-            if (!use_cond) J[2 * g.N + n + (b.ixs - i0)] = (T)jb;  // J keeps the last beam value
+    } else {
+        T lx[VEC], ly[VEC], lz[VEC];
+        if constexpr (MODE == 1) {
+            ldg_v<T, VEC>(lx, cl + n);
+            ldg_v<T, VEC>(ly, cl + g.N + n);
+            ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+        } else {
+            zero_v<T, VEC>(lx);
+            zero_v<T, VEC>(ly);
+            zero_v<T, VEC>(lz);
         }
+        epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, J, n, i0, j, k, use_cond, g, b, pl, st);
     }
     st_v<T, VEC>(E + n, ex);
     st_v<T, VEC>(E + g.N + n, ey);
     st_v<T, VEC>(E + 2 * g.N + n, ez);
+}
+
+// ---------------------------------------------------------------- staged kernels
+// Persistent kernels (one or two CTAs per SM) that walk the flat index space in chunks
+// of CH cells.  For every chunk one elected thread issues bulk copies
+// (cp.async.bulk global->shared, completion counted on an mbarrier) of each input
+// stream -- the chunk's own cells plus the +-Nx row and +-Nx*Ny plane neighbours and
+// a 16-byte pad for the +-1 neighbour -- into one of NST pipeline stages; the CTA
+// computes from shared memory while the next NST-1 chunks are in flight.  DRAM
+// latency is covered by the copies in flight, not by warp occupancy.  Requirements:
+// Nx*sizeof(T) is a multiple of 16 bytes (all stream starts are then 16-byte aligned).
+// Every wait is bounded: on expiry the kernel records FIT_ERR_TIMEOUT in *err, waits
+// (bounded) for its own copies and returns.
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// bounded wait on phase `parity`; returns false when the bound expired
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, long long max_iter) {
+    const unsigned a = smem_u32(bar);
+    for (long long it = 0; it < max_iter; ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+constexpr long long kWaitLimit = 1LL << 24;  // try_wait polls (each waits up to ~a microsecond)
+
+struct Stream {
+    int src;         // which input array (kernel specific)
+    int comp;        // component block
+    long long off;   // start relative to the chunk's first cell (elements)
+    int pad;         // extra elements (the +-1 neighbour), multiple of the 16-byte width
+};
+
+// issue the copies of one chunk; returns the bytes expected on the barrier
+template <typename T, int NS>
+__device__ __forceinline__ unsigned issue_chunk(const T* const* srcs, const Stream (&ss)[NS], long long n0, int CH,
+                                                long long N, T* stage, const int (&soff)[NS], unsigned long long* bar) {
+    unsigned total = 0;
+    long long beg[NS], end[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const long long a = n0 + ss[s].off;
+        beg[s] = a < 0 ? 0 : a;
+        long long e = a + CH + ss[s].pad;
+        end[s] = e > N ? N : e;
+        if (end[s] > beg[s]) total += (unsigned)((end[s] - beg[s]) * (long long)sizeof(T));
+    }
+    mbar_arrive_tx(bar, total);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        if (end[s] > beg[s]) {
+            const long long a = n0 + ss[s].off;
+            bulk_g2s(stage + soff[s] + (beg[s] - a), srcs[s] + (long long)ss[s].comp * N + beg[s],
+                     (unsigned)((end[s] - beg[s]) * (long long)sizeof(T)), bar);
+        }
+    }
+    return total;
+}
+
+template <typename T, int VEC>
+__device__ __forceinline__ void lds_v(T (&r)[VEC], const T* p) {
+    ld_v<T, VEC>(r, p);
+}
+
+// H pass streams: 0 Ex, 1 Ex+Nx, 2 Ex+NxNy, 3 Ey(+pad), 4 Ey+NxNy, 5 Ez(+pad), 6 Ez+Nx,
+// 7-9 H, 10-12 ch
+template <typename T, int VEC, int NST>
+__global__ void __launch_bounds__(256, 1) k_hpass_staged(const T* __restrict__ E, T* __restrict__ H,
+                                                         const T* __restrict__ ch, Geom g, Metric<T> mt, int* err) {
+    constexpr int A = 16 / sizeof(T);
+    constexpr int CH = 256 * VEC;
+    constexpr int NS = 13;
+    const Stream ss[NS] = {{0, 0, 0, 0},          {0, 0, g.sy, 0}, {0, 0, g.sz, 0}, {0, 1, 0, A}, {0, 1, g.sz, 0},
+                           {0, 2, 0, A},          {0, 2, g.sy, 0}, {1, 0, 0, 0},    {1, 1, 0, 0}, {1, 2, 0, 0},
+                           {2, 0, 0, 0},          {2, 1, 0, 0},    {2, 2, 0, 0}};
+    int soff[NS];
+    int stage_elems = 0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        soff[s] = stage_elems;
+        stage_elems += CH + ss[s].pad;
+    }
+    extern __shared__ __align__(128) unsigned char smem[];
+    T* buf = reinterpret_cast<T*>(smem);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + (size_t)NST * stage_elems * sizeof(T));
+    const T* srcs[NS] = {E, E, E, E, E, E, E, H, H, H, ch, ch, ch};
+    const long long nchunks = (g.N + CH - 1) / CH;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) {
+            const long long c = blockIdx.x + (long long)s * gridDim.x;
+            if (c < nchunks) issue_chunk<T, NS>(srcs, ss, c * CH, CH, g.N, buf + (size_t)s * stage_elems, soff, &bars[s]);
+        }
+    }
+    bool ok = true;
+    long long it = 0;
+    for (long long c = blockIdx.x; c < nchunks; c += gridDim.x, ++it) {
+        const int s = (int)(it % NST);
+        const unsigned parity = (unsigned)((it / NST) & 1);
+        // every thread waits; the decision to give up is CTA-uniform
+        if (!__syncthreads_and(mbar_wait(&bars[s], parity, kWaitLimit))) {
+            ok = false;
+            break;
+        }
+        const T* st = buf + (size_t)s * stage_elems;
+        const long long n0 = c * CH;
+        const long long n = n0 + (long long)tid * VEC;
+        if (n < g.N) {
+            int i0, j, k;
+            cell_of(n, g, i0, j, k);
+            const int o = tid * VEC;
+            T ex[VEC], ey[VEC], ez[VEC], exy[VEC], ezy[VEC], exz[VEC], eyz[VEC];
+            T hx[VEC], hy[VEC], hz[VEC], cx[VEC], cy[VEC], cz[VEC];
+            lds_v<T, VEC>(ex, st + soff[0] + o);
+            lds_v<T, VEC>(exy, st + soff[1] + o);
+            lds_v<T, VEC>(exz, st + soff[2] + o);
+            lds_v<T, VEC>(ey, st + soff[3] + o);
+            lds_v<T, VEC>(eyz, st + soff[4] + o);
+            lds_v<T, VEC>(ez, st + soff[5] + o);
+            lds_v<T, VEC>(ezy, st + soff[6] + o);
+            lds_v<T, VEC>(hx, st + soff[7] + o);
+            lds_v<T, VEC>(hy, st + soff[8] + o);
+            lds_v<T, VEC>(hz, st + soff[9] + o);
+            lds_v<T, VEC>(cx, st + soff[10] + o);
+            lds_v<T, VEC>(cy, st + soff[11] + o);
+            lds_v<T, VEC>(cz, st + soff[12] + o);
+            const T eyx = st[soff[3] + o + VEC];
+            const T ezx = st[soff[5] + o + VEC];
+            hpass_cells<T, VEC>(ex, ey, ez, exy, ezy, exz, eyz, eyx, ezx, hx, hy, hz, cx, cy, cz, i0, j, k, g, mt);
+            st_v<T, VEC>(H + n, hx);
+            st_v<T, VEC>(H + g.N + n, hy);
+            st_v<T, VEC>(H + 2 * g.N + n, hz);
+        }
+        __syncthreads();  // every thread is done with stage s
+        if (tid == 0) {
+            const long long cn = c + (long long)NST * gridDim.x;
+            if (cn < nchunks) {
+                fence_proxy_async();
+                issue_chunk<T, NS>(srcs, ss, cn * CH, CH, g.N, buf + (size_t)s * stage_elems, soff, &bars[s]);
+            }
+        }
+    }
+    if (!ok && tid == 0) {
+        atomicExch(err, FIT_ERR_TIMEOUT);
+        // drain: bounded waits on the stages of the chunks issued but not consumed
+        for (long long q = it; q < it + NST; ++q)
+            if (blockIdx.x + q * (long long)gridDim.x < nchunks)
+                mbar_wait(&bars[q % NST], (unsigned)((q / NST) & 1), kWaitLimit);
+    }
+}
+
+// E pass streams: 0 Hx, 1 Hx-Nx, 2 Hx-NxNy, 3 Hy(-pad), 4 Hy-NxNy, 5 Hz(-pad), 6 Hz-Nx,
+// 7-9 E, 10-12 ce, 13-15 cl (MODE 1)
+template <typename T, int VEC, int NST, int MODE>
+__global__ void __launch_bounds__(256, 1) k_epass_staged(T* __restrict__ E, const T* __restrict__ H,
+                                                         const T* __restrict__ ce, const T* __restrict__ cl,
+                                                         T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
+                                                         BeamArgs b, PlaneArgs pl, StepArgs stp, int* err) {
+    constexpr int A = 16 / sizeof(T);
+    constexpr int CH = 256 * VEC;
+    constexpr int NS = MODE == 1 ? 16 : 13;
+    Stream ss[NS];
+    {
+        const Stream base[16] = {{0, 0, 0, 0},      {0, 0, -g.sy, 0}, {0, 0, -g.sz, 0}, {0, 1, -A, A},
+                                 {0, 1, -g.sz, 0},  {0, 2, -A, A},    {0, 2, -g.sy, 0}, {1, 0, 0, 0},
+                                 {1, 1, 0, 0},      {1, 2, 0, 0},     {2, 0, 0, 0},     {2, 1, 0, 0},
+                                 {2, 2, 0, 0},      {3, 0, 0, 0},     {3, 1, 0, 0},     {3, 2, 0, 0}};
+#pragma unroll
+        for (int s = 0; s < NS; ++s) ss[s] = base[s];
+    }
+    int soff[NS];
+    int stage_elems = 0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        soff[s] = stage_elems;
+        stage_elems += CH + ss[s].pad;
+    }
+    extern __shared__ __align__(128) unsigned char smem[];
+    T* buf = reinterpret_cast<T*>(smem);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + (size_t)NST * stage_elems * sizeof(T));
+    const T* srcs[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        srcs[s] = s < 7 ? H : (s < 10 ? (const T*)E : (s < 13 ? ce : cl));
+    const long long nchunks = (g.N + CH - 1) / CH;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) {
+            const long long c = blockIdx.x + (long long)s * gridDim.x;
+            if (c < nchunks) issue_chunk<T, NS>(srcs, ss, c * CH, CH, g.N, buf + (size_t)s * stage_elems, soff, &bars[s]);
+        }
+    }
+    bool ok = true;
+    long long it = 0;
+    for (long long c = blockIdx.x; c < nchunks; c += gridDim.x, ++it) {
+        const int s = (int)(it % NST);
+        const unsigned parity = (unsigned)((it / NST) & 1);
+        // every thread waits; the decision to give up is CTA-uniform
+        if (!__syncthreads_and(mbar_wait(&bars[s], parity, kWaitLimit))) {
+            ok = false;
+            break;
+        }
+        const T* st = buf + (size_t)s * stage_elems;
+        const long long n0 = c * CH;
+        const long long n = n0 + (long long)tid * VEC;
+        if (n < g.N) {
+            int i0, j, k;
+            cell_of(n, g, i0, j, k);
+            const int o = tid * VEC;
+            T hx[VEC], hy[VEC], hz[VEC], hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
+            lds_v<T, VEC>(hx, st + soff[0] + o);
+            lds_v<T, VEC>(hxy, st + soff[1] + o);
+            lds_v<T, VEC>(hxz, st + soff[2] + o);
+            lds_v<T, VEC>(hy, st + soff[3] + A + o);
+            lds_v<T, VEC>(hyz, st + soff[4] + o);
+            lds_v<T, VEC>(hz, st + soff[5] + A + o);
+            lds_v<T, VEC>(hzy, st + soff[6] + o);
+            const T hyx = st[soff[3] + A + o - 1];
+            const T hzx = st[soff[5] + A + o - 1];
+            T cur[3][VEC];
+            epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
+            T ex[VEC], ey[VEC], ez[VEC], kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
+            lds_v<T, VEC>(ex, st + soff[7] + o);
+            lds_v<T, VEC>(ey, st + soff[8] + o);
+            lds_v<T, VEC>(ez, st + soff[9] + o);
+            lds_v<T, VEC>(kx, st + soff[10] + o);
+            lds_v<T, VEC>(ky, st + soff[11] + o);
+            lds_v<T, VEC>(kz, st + soff[12] + o);
+            if constexpr (MODE == 1) {
+                lds_v<T, VEC>(lx, st + soff[13] + o);
+                lds_v<T, VEC>(ly, st + soff[14] + o);
+                lds_v<T, VEC>(lz, st + soff[15] + o);
+            } else {
+                zero_v<T, VEC>(lx);
+                zero_v<T, VEC>(ly);
+                zero_v<T, VEC>(lz);
+            }
+            epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, J, n, i0, j, k, use_cond, g, b, pl,
+                                       stp);
+            st_v<T, VEC>(E + n, ex);
+            st_v<T, VEC>(E + g.N + n, ey);
+            st_v<T, VEC>(E + 2 * g.N + n, ez);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const long long cn = c + (long long)NST * gridDim.x;
+            if (cn < nchunks) {
+                fence_proxy_async();
+                issue_chunk<T, NS>(srcs, ss, cn * CH, CH, g.N, buf + (size_t)s * stage_elems, soff, &bars[s]);
+            }
+        }
+    }
+    if (!ok && tid == 0) {
+        atomicExch(err, FIT_ERR_TIMEOUT);
+        // drain: bounded waits on the stages of the chunks issued but not consumed
+        for (long long q = it; q < it + NST; ++q)
+            if (blockIdx.x + q * (long long)gridDim.x < nchunks)
+                mbar_wait(&bars[q % NST], (unsigned)((q / NST) & 1), kWaitLimit);
+    }
+}
+
+template <typename T, int VEC, int NS, int NST>
+constexpr size_t staged_smem_bytes() {
+    return (size_t)NST * ((size_t)NS * 256 * VEC + 2 * (16 / sizeof(T))) * sizeof(T) + NST * sizeof(unsigned long long);
 }
 
 // ---------------------------------------------------------------- coefficients

@@ -211,6 +211,7 @@ class RoutinesMixin:
         self._run_steps += nsteps
 
     def _after_device_run(self):
+        self._ctx.call("fit_check_error")  # raises FitError if a kernel gave up a bounded wait
         self._beam_armed = False
         if self.use_conductivity:
             self._j_state = "derived"
