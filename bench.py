@@ -206,6 +206,8 @@ def run_ours(args, rank, world):
     N = P.nx * P.ny * P.nz
     mask = P.walls_mask(device=dev)
     grid, wake, s = P.build(wg, mask)
+    if args.variant == "direct":
+        s._ctx.call("fit_set_kernel_variant", 0)
     del mask
     beam, Nt = s._wake_prepare(wake, P.wakelength, "both")
     vt = s._wake_device_setup(beam, Nt)
@@ -322,6 +324,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", type=int, nargs=3, default=None)
+    ap.add_argument("--variant", default="staged", choices=["staged", "direct"],
+                    help="pass kernels: persistent bulk-copy staged kernels or direct-load kernels")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

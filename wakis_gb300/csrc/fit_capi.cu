@@ -193,11 +193,12 @@ int launches_per_step(const FitCtx* c) {
 // staged kernels need 16-byte aligned stream starts: Nx*sizeof(T) % 16 == 0
 bool staged_ok(const FitCtx* c) { return c->staged && ((long long)c->g.nx * (long long)esize(c)) % 16 == 0; }
 
-constexpr int kNstH = 4, kNstE = 3;
+// pipeline stages and threads per CTA of the staged passes (one CTA per SM)
+constexpr int kNstH = 2, kTpbH = 512, kNstE = 2, kTpbE = 384;
 
-template <typename T, int VEC, int NS, int NST>
+template <typename T, int VEC, int NS, int NST, int TPB>
 size_t staged_bytes() {
-    return (size_t)NST * ((size_t)NS * 256 * VEC + 2 * (16 / sizeof(T))) * sizeof(T) + NST * sizeof(unsigned long long);
+    return (size_t)NST * ((size_t)NS * TPB * VEC + 2 * (16 / sizeof(T))) * sizeof(T) + NST * sizeof(unsigned long long);
 }
 
 template <typename KernelPtr>
@@ -208,10 +209,10 @@ void allow_smem(KernelPtr k, size_t bytes) {
 template <typename T, int VEC>
 void launch_h(FitCtx* c) {
     if (VEC * sizeof(T) == 16 && staged_ok(c)) {
-        const size_t sm = staged_bytes<T, VEC, 13, kNstH>();
-        auto k = k_hpass_staged<T, VEC, kNstH>;
+        const size_t sm = staged_bytes<T, VEC, 13, kNstH, kTpbH>();
+        auto k = k_hpass_staged<T, VEC, kNstH, kTpbH>;
         allow_smem(k, sm);
-        k<<<c->nsm, 256, sm, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
+        k<<<c->nsm, kTpbH, sm, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
                                        static_cast<const T*>(c->ch), c->g, metric<T>(c), c->d_err);
     } else {
         const long long nv = c->g.N / VEC;
@@ -232,16 +233,16 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
     const T* sg = static_cast<const T*>(c->sg);
     if (VEC * sizeof(T) == 16 && staged_ok(c) && mode != 2) {
         if (mode == 1) {
-            const size_t sm = staged_bytes<T, VEC, 16, kNstE>();
-            auto k = k_epass_staged<T, VEC, kNstE, 1>;
+            const size_t sm = staged_bytes<T, VEC, 16, kNstE, kTpbE>();
+            auto k = k_epass_staged<T, VEC, kNstE, 1, kTpbE>;
             allow_smem(k, sm);
-            k<<<c->nsm, 256, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
+            k<<<c->nsm, kTpbE, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
                                            c->d_err);
         } else {
-            const size_t sm = staged_bytes<T, VEC, 13, kNstE>();
-            auto k = k_epass_staged<T, VEC, kNstE, 0>;
+            const size_t sm = staged_bytes<T, VEC, 13, kNstE, kTpbE>();
+            auto k = k_epass_staged<T, VEC, kNstE, 0, kTpbE>;
             allow_smem(k, sm);
-            k<<<c->nsm, 256, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
+            k<<<c->nsm, kTpbE, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
                                            c->d_err);
         }
         count(c);
@@ -326,8 +327,8 @@ int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
         return fail(nullptr, FIT_ERR_ARG, "grid dimensions must be >= 1 (got %lld x %lld x %lld)",
                     (long long)d->nx, (long long)d->ny, (long long)d->nz);
     const long long N = d->nx * d->ny * d->nz;
-    if (3 * N >= (1LL << 31) * 2LL)
-        return fail(nullptr, FIT_ERR_ARG, "grid too large: 3*N = %lld", 3 * N);
+    if (N >= (1LL << 31))
+        return fail(nullptr, FIT_ERR_ARG, "grid too large: N = %lld cells (limit 2^31 - 1)", N);
     if (d->dtype != FIT_F32 && d->dtype != FIT_F64) return fail(nullptr, FIT_ERR_ARG, "dtype must be FIT_F32 or FIT_F64");
     for (int a = 0; a < 3; ++a)
         if (d->bc_lo[a] < 0 || d->bc_lo[a] > 4 || d->bc_hi[a] < 0 || d->bc_hi[a] > 4)
@@ -346,6 +347,8 @@ int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
     c->g.N = N;
     c->g.sy = d->nx;
     c->g.sz = d->nx * d->ny;
+    c->g.fx = make_fastdiv((unsigned)d->nx);
+    c->g.fy = make_fastdiv((unsigned)d->ny);
     // face masks (wakis/boundaries.py:73-150)
     unsigned pec = 0, pmc = 0;
     bool any_pmc = false;

@@ -16,6 +16,31 @@
 
 namespace fit {
 
+// Unsigned 32-bit division by an invariant divisor d with one multiply-high
+// (Granlund & Montgomery, "Division by invariant integers using multiplication", 1994,
+// Fig. 4.1): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// q = (t + ((n - t) >> min(l,1))) >> max(l-1,0) with t = mulhi(m, n); exact for n < 2^32.
+struct FastDiv {
+    unsigned d, m;
+    int s1, s2;
+};
+
+inline FastDiv make_fastdiv(unsigned d) {
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    FastDiv f;
+    f.d = d;
+    f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l - 1 > 0 ? l - 1 : 0;
+    return f;
+}
+
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv& f) {
+    const unsigned t = __umulhi(f.m, n);
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 // face bit f: 0 x-lo, 1 x-hi, 2 y-lo, 3 y-hi, 4 z-lo, 5 z-hi
 struct Geom {
     int nx, ny, nz;
@@ -25,7 +50,15 @@ struct Geom {
     long long sz;  // Nx*Ny
     unsigned pec;  // faces whose tangential E columns are zeroed (Dbc of PEC/PML)
     unsigned pmc;  // faces whose tangential H rows/columns are zeroed (Dbc of PMC)
+    FastDiv fx, fy;  // division by Nx and by Ny
 };
+
+// A thread's VEC cells (i0..i0+VEC-1, j, k) and all their +-1 neighbours lie at least one
+// cell away from every face: no face mask, no row crossing, no truncation applies.
+template <int VEC>
+__device__ __forceinline__ bool interior(int i0, int j, int k, const Geom& g) {
+    return i0 >= 2 && i0 + VEC + 2 <= g.nx && j >= 2 && j + 3 <= g.ny && k >= 2 && k + 3 <= g.nz;
+}
 
 // Dbc face mask of component d at (i, j, k).  The reference writes the mask plane by
 // plane in the order x-lo, x-hi, y-lo, y-hi, z-lo, z-hi skipping the component's own
@@ -231,6 +264,23 @@ __device__ __forceinline__ void hpass_cells(const T (&ex)[VEC], const T (&ey)[VE
                                             T (&hz)[VEC], const T (&cx)[VEC], const T (&cy)[VEC],
                                             const T (&cz)[VEC], int i0, int j, int k, const Geom& g,
                                             const Metric<T>& mt) {
+    if (interior<VEC>(i0, j, k, g)) {
+        // all masks open, edge lengths separable: L_x(i), L_y(j), L_z(k)
+        const T ly = mt.L[1][j], lz = mt.L[2][k];
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const T lx = mt.L[0][i0 + e];
+            const T eyX = (e + 1 < VEC) ? ey[e + 1] : eyx;
+            const T ezX = (e + 1 < VEC) ? ez[e + 1] : ezx;
+            const T curlx = ly * (ey[e] - eyz[e]) + lz * (ezy[e] - ez[e]);
+            const T curly = lx * (exz[e] - ex[e]) + lz * (ez[e] - ezX);
+            const T curlz = lx * (ex[e] - exy[e]) + ly * (eyX - ey[e]);
+            hx[e] = hx[e] - cx[e] * curlx;
+            hy[e] = hy[e] - cy[e] * curly;
+            hz[e] = hz[e] - cz[e] * curlz;
+        }
+        return;
+    }
     const Nb xl = fwd_x(i0 + VEC - 1, j, k, g);
     const Nb py = fwd_y(i0, j, k, g);
     const Nb pz = fwd_z(i0, j, k, g);
@@ -266,6 +316,19 @@ __device__ __forceinline__ void epass_curl(const T (&hx)[VEC], const T (&hy)[VEC
                                            const T (&hxy)[VEC], const T (&hzy)[VEC], const T (&hxz)[VEC],
                                            const T (&hyz)[VEC], T hyx, T hzx, T (&cur)[3][VEC], int i0, int j,
                                            int k, const Geom& g, const Metric<T>& mt) {
+    if (interior<VEC>(i0, j, k, g)) {
+        const T ly = mt.tL[1][j], lz = mt.tL[2][k];
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const T lx = mt.tL[0][i0 + e];
+            const T hyX = (e > 0) ? hy[e - 1] : hyx;
+            const T hzX = (e > 0) ? hz[e - 1] : hzx;
+            cur[0][e] = ly * (hyz[e] - hy[e]) + lz * (hz[e] - hzy[e]);
+            cur[1][e] = lx * (hx[e] - hxz[e]) + lz * (hzX - hz[e]);
+            cur[2][e] = lx * (hxy[e] - hx[e]) + ly * (hy[e] - hyX);
+        }
+        return;
+    }
     const Nb xf = bwd_x(i0, j, k, g);
     const Nb py = bwd_y(i0, j, k, g);
     const Nb pz = bwd_z(i0, j, k, g);
@@ -343,11 +406,14 @@ __device__ __forceinline__ void epass_update(T (&ex)[VEC], T (&ey)[VEC], T (&ez)
     }
 }
 
+// (i, j, k) of the component-local flat index n (N < 2^31 is checked on the host)
 __device__ __forceinline__ void cell_of(long long n, const Geom& g, int& i0, int& j, int& k) {
-    i0 = (int)(n % g.nx);
-    const long long r = n / g.nx;
-    j = (int)(r % g.ny);
-    k = (int)(r / g.ny);
+    const unsigned u = (unsigned)n;
+    const unsigned r = fdiv(u, g.fx);
+    i0 = (int)(u - r * (unsigned)g.nx);
+    const unsigned q = fdiv(r, g.fy);
+    j = (int)(r - q * (unsigned)g.ny);
+    k = (int)q;
 }
 
 // ---------------------------------------------------------------- direct kernels
@@ -612,11 +678,11 @@ __device__ __forceinline__ void lds_v(T (&r)[VEC], const T* p) {
 
 // H pass streams: 0 Ex, 1 Ex+Nx, 2 Ex+NxNy, 3 Ey(+pad), 4 Ey+NxNy, 5 Ez(+pad), 6 Ez+Nx,
 // 7-9 H, 10-12 ch
-template <typename T, int VEC, int NST>
-__global__ void __launch_bounds__(256, 1) k_hpass_staged(const T* __restrict__ E, T* __restrict__ H,
+template <typename T, int VEC, int NST, int TPB>
+__global__ void __launch_bounds__(TPB, 1) k_hpass_staged(const T* __restrict__ E, T* __restrict__ H,
                                                          const T* __restrict__ ch, Geom g, Metric<T> mt, int* err) {
     constexpr int A = 16 / sizeof(T);
-    constexpr int CH = 256 * VEC;
+    constexpr int CH = TPB * VEC;
     constexpr int NS = 13;
     const Stream ss[NS] = {{0, 0, 0, 0},          {0, 0, g.sy, 0}, {0, 0, g.sz, 0}, {0, 1, 0, A}, {0, 1, g.sz, 0},
                            {0, 2, 0, A},          {0, 2, g.sy, 0}, {1, 0, 0, 0},    {1, 1, 0, 0}, {1, 2, 0, 0},
@@ -704,13 +770,13 @@ __global__ void __launch_bounds__(256, 1) k_hpass_staged(const T* __restrict__ E
 
 // E pass streams: 0 Hx, 1 Hx-Nx, 2 Hx-NxNy, 3 Hy(-pad), 4 Hy-NxNy, 5 Hz(-pad), 6 Hz-Nx,
 // 7-9 E, 10-12 ce, 13-15 cl (MODE 1)
-template <typename T, int VEC, int NST, int MODE>
-__global__ void __launch_bounds__(256, 1) k_epass_staged(T* __restrict__ E, const T* __restrict__ H,
+template <typename T, int VEC, int NST, int MODE, int TPB>
+__global__ void __launch_bounds__(TPB, 1) k_epass_staged(T* __restrict__ E, const T* __restrict__ H,
                                                          const T* __restrict__ ce, const T* __restrict__ cl,
                                                          T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
                                                          BeamArgs b, PlaneArgs pl, StepArgs stp, int* err) {
     constexpr int A = 16 / sizeof(T);
-    constexpr int CH = 256 * VEC;
+    constexpr int CH = TPB * VEC;
     constexpr int NS = MODE == 1 ? 16 : 13;
     Stream ss[NS];
     {
@@ -815,11 +881,6 @@ __global__ void __launch_bounds__(256, 1) k_epass_staged(T* __restrict__ E, cons
             if (blockIdx.x + q * (long long)gridDim.x < nchunks)
                 mbar_wait(&bars[q % NST], (unsigned)((q / NST) & 1), kWaitLimit);
     }
-}
-
-template <typename T, int VEC, int NS, int NST>
-constexpr size_t staged_smem_bytes() {
-    return (size_t)NST * ((size_t)NS * 256 * VEC + 2 * (16 / sizeof(T))) * sizeof(T) + NST * sizeof(unsigned long long);
 }
 
 // ---------------------------------------------------------------- coefficients
