@@ -83,7 +83,7 @@ struct FitCtx {
     bool capturing = false;
     int* d_err = nullptr;   // device error word written by kernels (FIT_ERR_TIMEOUT)
     int nsm = 1;            // SM count: grid of the persistent staged kernels
-    bool staged = true;     // staged (bulk-copy) passes when the grid is aligned
+    bool staged = false;    // staged (bulk-copy) passes when the grid is aligned (opt-in)
     std::string err;
 };
 

@@ -420,7 +420,7 @@ __device__ __forceinline__ void cell_of(long long n, const Geom& g, int& i0, int
 // One thread per VEC cells, inputs loaded straight from global memory.  Used for grids
 // whose Nx is not a multiple of the 16-byte vector width and for the explicit-J pass.
 template <typename T, int VEC>
-__global__ void __launch_bounds__(256) k_hpass(const T* __restrict__ E, T* __restrict__ H,
+__global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __restrict__ H,
                                                const T* __restrict__ ch, Geom g, Metric<T> mt) {
     const long long nvec = g.N / VEC;
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -475,7 +475,7 @@ __global__ void __launch_bounds__(256) k_hpass(const T* __restrict__ E, T* __res
 // MODE 2: E = E + ce*(C^T ĥ) - cj*J; J = sg*E   (explicit J; J written if conductive)
 // The beam line (ixs, iys, :) of the z component uses the beam current instead of J.
 template <typename T, int VEC, int MODE>
-__global__ void __launch_bounds__(256) k_epass(T* __restrict__ E, const T* __restrict__ H,
+__global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __restrict__ H,
                                                const T* __restrict__ ce, const T* __restrict__ cl,
                                                T* __restrict__ J, const T* __restrict__ cj,
                                                const T* __restrict__ sg, int use_cond, Geom g,
