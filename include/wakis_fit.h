@@ -176,6 +176,23 @@ FIT_API int fit_wake_finalize(FitCtx *ctx, double qscale, double ds, double dxf,
 FIT_API int fit_dft(const double *x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
             double *out);
 
+/* Allocation-free variant of fit_dft; it has no counterpart in the reference.  For callers
+ * that cannot allocate device memory when they need a spectrum: a process whose device
+ * memory is all owned by its own pool (field storage of many concurrent solves), or one
+ * that must not take the device-wide synchronisation of cudaMalloc / cudaFree while
+ * kernels run on other streams.  x (device, nsig*len FP64, signal-major) and out (device,
+ * nsig*nb (re, im) FP64 pairs) belong to the caller; the work is queued on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and the call returns without waiting.
+ * Partial sums live in one fixed file-scope device array of 2^18 double2 (4 MiB) that every
+ * GPU loading this library holds until the process exits: nsig*nb must not exceed 2^18
+ * (FIT_ERR_ARG otherwise).  The array keeps the last call's contents; every entry a call
+ * reads is written earlier in the same call, so nothing is cleared.  All calls on a device
+ * share the array: calls that overlap on the GPU race.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture.  Errors: fit_last_error(NULL, ...). */
+FIT_API int fit_dft_noalloc(const double *x, int32_t nsig, int64_t len, int64_t n, int64_t b0,
+                            int32_t nb, double *out, void *stream);
+
 /* Reads the context's device error word (synchronizes the context stream): FIT_OK, or
  * FIT_ERR_TIMEOUT when a kernel gave up a bounded wait on its bulk copies (the kernel
  * then returned without completing its pass).  The word is cleared by the read. */

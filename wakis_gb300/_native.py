@@ -68,6 +68,7 @@ _SIGS = {
     "fit_dft": (_D, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _D),
     "fit_time_kernels": (_P, C.c_int32, _D),
     "fit_check_error": (_P,),
+    "fit_dft_noalloc": (_P, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P, _P),
     "fit_set_kernel_variant": (_P, C.c_int32),
     "fit_version": (C.c_char_p, C.c_int64),
     "fit_launch_count": (),

@@ -977,3 +977,69 @@ int fit_version(char* buf, int64_t len) {
 int64_t fit_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free DFT.  Some callers cannot allocate device memory at the moment they need
+// an impedance spectrum: a serving process that has handed all of HBM to a pool it manages
+// itself (field storage for many concurrent solves), or a caller that must not pay the
+// device-wide synchronisation that cudaMalloc / cudaFree imply while solver kernels are
+// running on other streams.  fit_dft_noalloc takes device inputs and outputs from the
+// caller and keeps its partial sums in a fixed file-scope device array instead of
+// allocating.  That array (kDftScratchEntries double2 = 4 MiB) is resident on every GPU
+// that loads this library until the process exits; every call on a device shares it.
+namespace {
+
+constexpr long long kDftScratchEntries = 1LL << 18;  // double2 partial sums (4 MiB)
+__device__ __align__(256) double2 g_dft_scratch[kDftScratchEntries];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double2* g_scratch_ptr[kMaxDevices] = {};
+
+// device address of g_dft_scratch on the current device, looked up once per device
+// (host code only sees a host-side stand-in for the symbol)
+int scratch_address(int dev, double2** out) {
+    if (dev < 0 || dev >= kMaxDevices) return fail(nullptr, FIT_ERR_DEVICE, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_dft_scratch);
+        if (e != cudaSuccess)
+            return fail(nullptr, FIT_ERR_CUDA, "cudaGetSymbolAddress(g_dft_scratch) failed: %s", cudaGetErrorString(e));
+        g_scratch_ptr[dev] = static_cast<double2*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return FIT_OK;
+}
+
+}  // namespace
+
+extern "C" int fit_dft_noalloc(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
+                               double* out, void* stream) {
+    if (!x || !out || nsig <= 0 || len <= 0 || n <= 0 || nb <= 0 || b0 < 0)
+        return fail(nullptr, FIT_ERR_ARG, "bad fit_dft_noalloc arguments");
+    const long long per_split = (long long)nsig * nb;
+    if (per_split > kDftScratchEntries)
+        return fail(nullptr, FIT_ERR_ARG,
+                    "fit_dft_noalloc: nsig*nb = %lld exceeds the fixed scratch of %lld partial sums", per_split,
+                    kDftScratchEntries);
+    int nsplit = (int)std::max<long long>(1, std::min<long long>(32, len / 2048));
+    while ((long long)nsplit * per_split > kDftScratchEntries && nsplit > 1) --nsplit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "cudaGetDevice failed: %s", cudaGetErrorString(e));
+    double2* part = nullptr;
+    int rc = scratch_address(dev, &part);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // every partial read by the reduction is written by this call's first kernel, so the
+    // scratch needs no clearing; calls that overlap on the GPU share it and race
+    dim3 grid((unsigned)nb, (unsigned)nsig, (unsigned)nsplit);
+    k_dft_partial<<<grid, 256, 0, s>>>(x, nsig, len, n, b0, nb, nsplit, part);
+    k_dft_reduce<<<grid1d((long long)nsig * nb, 256), 256, 0, s>>>(part, nsig, nb, nsplit,
+                                                                  reinterpret_cast<double2*>(out));
+    g_launches += 2;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "fit_dft_noalloc launch failed: %s", cudaGetErrorString(e));
+    return FIT_OK;
+}
