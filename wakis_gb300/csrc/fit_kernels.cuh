@@ -60,6 +60,14 @@ __device__ __forceinline__ bool interior(int i0, int j, int k, const Geom& g) {
     return i0 >= 2 && i0 + VEC + 2 <= g.nx && j >= 2 && j + 3 <= g.ny && k >= 2 && k + 3 <= g.nz;
 }
 
+// Row (j, k) at least two cells from the y and z faces: neighbours along y and z stay in
+// the block, no y/z face mask applies, and the only row crossing is the x one.  All
+// threads of a warp share one row on grids with Nx >= 32*VEC, so this test does not
+// split warps there.
+__device__ __forceinline__ bool row_interior(int j, int k, const Geom& g) {
+    return j >= 2 && j + 3 <= g.ny && k >= 2 && k + 3 <= g.nz;
+}
+
 // Dbc face mask of component d at (i, j, k).  The reference writes the mask plane by
 // plane in the order x-lo, x-hi, y-lo, y-hi, z-lo, z-hi skipping the component's own
 // axis, so the LAST applicable write wins (wakis/boundaries.py:92-101): test in
@@ -264,17 +272,28 @@ __device__ __forceinline__ void hpass_cells(const T (&ex)[VEC], const T (&ey)[VE
                                             T (&hz)[VEC], const T (&cx)[VEC], const T (&cy)[VEC],
                                             const T (&cz)[VEC], int i0, int j, int k, const Geom& g,
                                             const Metric<T>& mt) {
-    if (interior<VEC>(i0, j, k, g)) {
-        // all masks open, edge lengths separable: L_x(i), L_y(j), L_z(k)
+    if (row_interior(j, k, g)) {
+        // j and k at least 2 cells from the y / z faces: the only masks are those of the
+        // x faces on the y, z components, and the only crossing is the x neighbour of
+        // i = Nx-1, which is (0, j+1, k).  Edge lengths: L_x(i), L_y(j), L_z(k).
         const T ly = mt.L[1][j], lz = mt.L[2][k];
+        const bool xlo = g.pec & 1u, xhi = (g.pec >> 1) & 1u;
+        const int il = i0 + VEC;
+        const bool cross = il >= g.nx;
+        const T mlast = cross ? (xlo ? T(0) : T(1)) : (((il == g.nx - 1) && xhi) ? T(0) : T(1));
+        const T lyl = cross ? mt.L[1][j + 1] : ly;
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
-            const T lx = mt.L[0][i0 + e];
+            const int i = i0 + e;
+            const T lx = mt.L[0][i];
+            const T me = (((i == 0) && xlo) || ((i == g.nx - 1) && xhi)) ? T(0) : T(1);
+            const T mn = (e + 1 < VEC) ? ((((i + 1) == g.nx - 1) && xhi) ? T(0) : T(1)) : mlast;
+            const T lyn = (e + 1 < VEC) ? ly : lyl;
             const T eyX = (e + 1 < VEC) ? ey[e + 1] : eyx;
             const T ezX = (e + 1 < VEC) ? ez[e + 1] : ezx;
-            const T curlx = ly * (ey[e] - eyz[e]) + lz * (ezy[e] - ez[e]);
-            const T curly = lx * (exz[e] - ex[e]) + lz * (ez[e] - ezX);
-            const T curlz = lx * (ex[e] - exy[e]) + ly * (eyX - ey[e]);
+            const T curlx = me * (ly * (ey[e] - eyz[e]) + lz * (ezy[e] - ez[e]));
+            const T curly = lx * (exz[e] - ex[e]) + lz * (me * ez[e] - mn * ezX);
+            const T curlz = lx * (ex[e] - exy[e]) + (mn * lyn * eyX - me * ly * ey[e]);
             hx[e] = hx[e] - cx[e] * curlx;
             hy[e] = hy[e] - cy[e] * curly;
             hz[e] = hz[e] - cz[e] * curlz;
@@ -316,16 +335,26 @@ __device__ __forceinline__ void epass_curl(const T (&hx)[VEC], const T (&hy)[VEC
                                            const T (&hxy)[VEC], const T (&hzy)[VEC], const T (&hxz)[VEC],
                                            const T (&hyz)[VEC], T hyx, T hzx, T (&cur)[3][VEC], int i0, int j,
                                            int k, const Geom& g, const Metric<T>& mt) {
-    if (interior<VEC>(i0, j, k, g)) {
+    if (row_interior(j, k, g)) {
+        // PMC masks of the x faces on the y, z components; the x neighbour of i = 0 is
+        // (Nx-1, j-1, k).  Dual lengths: tL_x(i), tL_y(j), tL_z(k).
         const T ly = mt.tL[1][j], lz = mt.tL[2][k];
+        const bool plo = g.pmc & 1u, phi = (g.pmc >> 1) & 1u;
+        const bool cross = i0 == 0;
+        const T mfirst = cross ? (phi ? T(0) : T(1)) : ((((i0 - 1) == 0) && plo) ? T(0) : T(1));
+        const T lyf = cross ? mt.tL[1][j - 1] : ly;
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
-            const T lx = mt.tL[0][i0 + e];
+            const int i = i0 + e;
+            const T lx = mt.tL[0][i];
+            const T mpe = (((i == 0) && plo) || ((i == g.nx - 1) && phi)) ? T(0) : T(1);
+            const T mpp = (e > 0) ? ((((i - 1) == 0) && plo) ? T(0) : T(1)) : mfirst;
+            const T lyp = (e > 0) ? ly : lyf;
             const T hyX = (e > 0) ? hy[e - 1] : hyx;
             const T hzX = (e > 0) ? hz[e - 1] : hzx;
-            cur[0][e] = ly * (hyz[e] - hy[e]) + lz * (hz[e] - hzy[e]);
-            cur[1][e] = lx * (hx[e] - hxz[e]) + lz * (hzX - hz[e]);
-            cur[2][e] = lx * (hxy[e] - hx[e]) + ly * (hy[e] - hyX);
+            cur[0][e] = mpe * (ly * (hyz[e] - hy[e]) + lz * (hz[e] - hzy[e]));
+            cur[1][e] = lx * (hx[e] - hxz[e]) + lz * (mpp * hzX - mpe * hz[e]);
+            cur[2][e] = lx * (hxy[e] - hx[e]) + (mpe * ly * hy[e] - mpp * lyp * hyX);
         }
         return;
     }
