@@ -301,6 +301,91 @@ def e2e(wg, torch, dev, P):
             "what": "GridFIT3D + SolverFIT3D setup from a host mask, wakesolve(0.3 m), WakeSolver results on host"}
 
 
+def _rel(a, b, ref=None):
+    a, b = np.asarray(a, dtype=np.complex128), np.asarray(b, dtype=np.complex128)
+    den = np.linalg.norm(b)
+    if ref is not None:
+        den = max(den, 1e-3 * np.linalg.norm(np.asarray(ref, dtype=np.complex128)))
+    return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+
+
+def run_accuracy(args):
+    """FP32 runs against the FP64 CUDA path (validated against the CPU oracle at 1e-10):
+    config 1 (both beam runs: fields, WP, WPx, WPy, Z, Zx, Zy), config 2 (64 probes of
+    Ez over 2000 steps) and, with --accuracy-cfg4, config 4 (WP over the first 0.3 m)."""
+    import torch
+    import wakis_gb300 as wg
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import cases as CS
+    from product_runner import make_grid, make_solver
+    out = {}
+    tmp = tempfile.mkdtemp()
+    for name in ("config1a", "config1b"):
+        case = CS.CONFIGS[name]
+        res = {}
+        for dt in (np.float32, np.float64):
+            grid = make_grid(wg, case)
+            wake = wg.WakeSolver(wakelength=case["wakelength"], save=False, verbose=0, results_folder=tmp,
+                                 **case["wake"])
+            s = make_solver(wg, case, grid, wake, dt)
+            t0 = time.perf_counter()
+            s.wakesolve(wakelength=case["wakelength"])
+            torch.cuda.synchronize()
+            res[dt] = dict(sec=time.perf_counter() - t0, Nt=s.Nt, s=wake.s, WP=wake.WP, WPx=wake.WPx, WPy=wake.WPy,
+                           Z=wake.Z, Zx=wake.Zx, Zy=wake.Zy, E=s.E.numpy(), H=s.H.numpy())
+            del s, grid, wake
+        a, b = res[np.float32], res[np.float64]
+        n = min(len(a["WP"]), len(b["WP"]))
+        m = min(len(a["Z"]), len(b["Z"]))
+        out[name] = {"Nt_fp32": a["Nt"], "Nt_fp64": b["Nt"], "seconds_fp32": a["sec"], "seconds_fp64": b["sec"],
+                     "WP": _rel(a["WP"][:n], b["WP"][:n]), "WPx": _rel(a["WPx"][:n], b["WPx"][:n], b["WP"][:n]),
+                     "WPy": _rel(a["WPy"][:n], b["WPy"][:n], b["WP"][:n]), "Z": _rel(a["Z"][:m], b["Z"][:m]),
+                     "Zx": _rel(a["Zx"][:m], b["Zx"][:m], b["Z"][:m]), "Zy": _rel(a["Zy"][:m], b["Zy"][:m], b["Z"][:m]),
+                     "E": _rel(a["E"], b["E"]), "H": _rel(a["H"], b["H"])}
+    # config 2: probes
+    case = CS.CONFIGS["config2"]
+    P = CS.probe_points(case)
+    probes = {}
+    for dt in (np.float32, np.float64):
+        grid = make_grid(wg, case)
+        s = make_solver(wg, case, grid, dtype=dt)
+        sc = case["source"]
+        src = wg.sources.WavePacket(zs=sc["zs"], sigmaz=sc["sigmaz"], sigmaxy=sc["sigmaxy"],
+                                    wavelength=sc["wavelength"], amplitude=sc["amplitude"])
+        flat = torch.as_tensor(2 * s.N + P[:, 0] + s.Nx * P[:, 1] + s.Nx * s.Ny * P[:, 2], device=s.E.array.device)
+        rec = []
+        t0 = time.perf_counter()
+        s.emsolve(case["Nt"], source=src, callback=lambda sv, t: rec.append(sv.E.array[flat].double()))
+        torch.cuda.synchronize()
+        probes[dt] = (torch.stack(rec).cpu().numpy(), time.perf_counter() - t0)
+        del s, grid
+    out["config2"] = {"probe_Ez_rel_l2": _rel(probes[np.float32][0], probes[np.float64][0]),
+                      "probe_Ez_max_abs_over_max": float(np.abs(probes[np.float32][0] - probes[np.float64][0]).max()
+                                                         / np.abs(probes[np.float64][0]).max()),
+                      "steps": case["Nt"], "probes": int(len(P))}
+    if args.accuracy_cfg4:
+        P4 = Pillbox()
+        res = {}
+        for dt in (np.float32, np.float64):
+            mask = P4.walls_mask(device=torch.device("cuda", 0))
+            grid, wake, s = P4.build(wg, mask, dtype=dt)
+            del mask
+            t0 = time.perf_counter()
+            s.wakesolve(wakelength=P4.wakelength)
+            torch.cuda.synchronize()
+            res[dt] = dict(sec=time.perf_counter() - t0, s=wake.s, WP=wake.WP, Z=wake.Z, Nt=s.Nt)
+            del s, grid, wake
+            import gc
+            gc.collect()
+            torch.cuda.empty_cache()
+        a, b = res[np.float32], res[np.float64]
+        n = min(len(a["WP"]), len(b["WP"]))
+        out["config4"] = {"WP_first_0.3m": _rel(a["WP"][:n], b["WP"][:n]), "Z": _rel(a["Z"], b["Z"]),
+                          "Nt": a["Nt"], "seconds_fp32": a["sec"], "seconds_fp64": b["sec"]}
+    print(json.dumps({"accuracy": out}), flush=True)
+
+
 def profile_traffic():
     """DRAM bytes per E-pass launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "epass_cfg4_ncu.md")
@@ -324,6 +409,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", type=int, nargs=3, default=None)
+    ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 errors on configs 1, 2 (and 4)")
+    ap.add_argument("--accuracy-cfg4", action="store_true")
     ap.add_argument("--variant", default="staged", choices=["staged", "direct"],
                     help="pass kernels: persistent bulk-copy staged kernels or direct-load kernels")
     args = ap.parse_args()
@@ -332,7 +419,9 @@ def main():
     if world > 1 and args.impl == "ours":
         import torch
         torch.distributed.init_process_group("nccl")
-    if args.impl == "reference":
+    if args.accuracy or args.accuracy_cfg4:
+        run_accuracy(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world)

@@ -221,3 +221,43 @@ def resonator_H(N, dt):
     Hx = (-2 / h2 * (m * np.pi / L) * (p * np.pi / L) * np.sin(m * np.pi / L * (X - L / 2))
           * np.cos(n * np.pi / L * (Y - L / 2)) * np.cos(p * np.pi / L * (Z - L / 2)) * ct)
     return Hx, Hy, Hz, (xmin, xmin + L)
+
+
+# ----------------------------------------------------------------------------- full configs
+# The BASELINE workloads at full size (geometry analytic, evaluated at cell centres).
+CONFIGS = {
+    # config 0: plain FP64 PEC cubic cavity, 60x60x120, ABC in z, CFL 1.0, wake 0.5 m, fmax 5 GHz
+    "config0": dict(
+        kind="wake", dtype="float64", grid=dict(_cavity_grid, Nx=60, Ny=60, Nz=120),
+        solids=[("cavity", "cube_pipe", {}, [1.0, 1.0])], bg="pec",
+        bc_low=["pec", "pec", "abc"], bc_high=["pec", "pec", "abc"], cfln=1.0,
+        wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
+                  fmax=5e9, skip_cells=0),
+        wakelength=0.5, compute_plane="both"),
+    # config 1, run a: 128x128x256, sigma = 1e4 walls (relaxation form), 10-cell z PML, beta 1
+    # (CFL 0.5: the reference's explicit loss term diverges at CFL 1.0 with sigma > 0 cells)
+    "config1a": dict(
+        kind="wake", dtype="float32", grid=dict(_cavity_grid, Nx=128, Ny=128, Nz=256),
+        solids=[("walls", "walls", {}, [1.0, 1.0, 1e4])], bg=[1.0, 1.0],
+        bc_low=["pec", "pec", "pml"], bc_high=["pec", "pec", "pml"], n_pml=10, cfln=0.5,
+        wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
+                  fmax=5e9, skip_cells=0),
+        wakelength=1.0, compute_plane="both"),
+    # config 1, run b: beta 0.8, source and test offset 2 mm in x
+    "config1b": dict(
+        kind="wake", dtype="float32", grid=dict(_cavity_grid, Nx=128, Ny=128, Nz=256),
+        solids=[("walls", "walls", {}, [1.0, 1.0, 1e4])], bg=[1.0, 1.0],
+        bc_low=["pec", "pec", "pml"], bc_high=["pec", "pec", "pml"], n_pml=10, cfln=0.5,
+        wake=dict(q=1e-9, sigmaz=10 * MM, beta=0.8, xsource=2 * MM, ysource=0.0, xtest=2 * MM, ytest=0.0,
+                  fmax=5e9, skip_cells=0),
+        wakelength=1.0, compute_plane="both"),
+    # config 2: unit box [-1,1]^3 on 256^3, 12-cell PML on all faces, sphere r=0.25 eps_r=2,
+    # x-polarised wave packet along +z, centre wavelength 0.2, 2000 steps, 64 probes
+    "config2": dict(
+        kind="emsolve", dtype="float32",
+        grid=dict(xmin=-1.0, xmax=1.0, ymin=-1.0, ymax=1.0, zmin=-1.0, zmax=1.0, Nx=256, Ny=256, Nz=256),
+        solids=[("sphere", "sphere", {"R": 0.25}, [2.0, 1.0])], bg=[1.0, 1.0],
+        bc_low=["pml", "pml", "pml"], bc_high=["pml", "pml", "pml"], n_pml=12, cfln=0.5,
+        source=dict(type="WavePacket", zs=13, sigmaz=0.3, sigmaxy=100.0, wavelength=0.2, amplitude=1.0),
+        Nt=2000, probes=64),
+}

@@ -1,0 +1,79 @@
+"""Parity and accuracy at the BASELINE workloads themselves (full size):
+
+* config 0 (FP64, 60x60x120, 1220 steps): the CUDA path against the CPU oracle within
+  1e-10 relative L2 on WP, Z and the final fields;
+* the reference's own tests/test_001 golden vectors (FP32, 50x50x150, 5184 steps) with
+  the tolerances of that test, and against the reference's full run of the same case;
+* config 1 (128x128x256 lossy, both beam runs): FP32 against the FP64 CUDA path (itself
+  checked against the oracle at 1e-10 on the smaller cases) -- WP within 1e-4.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import cases as C
+from oracle_runner import load_golden, rel_l2, run_oracle_case
+from product_runner import run_case
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def test_config0_fp64_matches_oracle(tmp_path):
+    case = C.CONFIGS["config0"]
+    got = run_case("config0", case=case, tmpdir=tmp_path)
+    ref = run_oracle_case("config0", case=case)
+    assert int(got["Nt"]) == int(ref["Nt"])
+    np.testing.assert_array_equal(got["s"], ref["s"])
+    np.testing.assert_array_equal(got["f"], ref["f"])
+    for k in ("WP", "Z", "E", "H", "WP_3d"):
+        assert rel_l2(got[k], ref[k]) < 1e-10, (k, rel_l2(got[k], ref[k]))
+    for k, r in (("WPx", "WP"), ("WPy", "WP"), ("Zx", "Z"), ("Zy", "Z")):
+        e = np.linalg.norm(got[k] - ref[k]) / max(np.linalg.norm(ref[k]), 1e-3 * np.linalg.norm(ref[r]))
+        assert e < 1e-10, (k, e)
+
+
+def test_reference_test001_goldens_on_gpu(tmp_path):
+    import wakis_gb300 as wg
+    z = load_golden("test001")
+    b = z["bounds"]
+    x = np.linspace(b[0], b[1], 51)
+    y = np.linspace(b[2], b[3], 51)
+    zz = np.linspace(b[4], b[5], 151)
+    tol = 1e-3 * min(np.diff(x).min(), np.diff(y).min(), np.diff(zz).min())
+    mask = C.test001_boxes_corner_rule(x, y, zz, tol)
+    grid = wg.GridFIT3D(*b, 50, 50, 150, stl_solids={"cavity": mask}, stl_materials={"cavity": "vacuum"}, verbose=0)
+    wake = wg.WakeSolver(wakelength=1.0, q=1e-9, sigmaz=18.5e-3, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0,
+                         ytest=0.0, save=False, skip_cells=12, verbose=0, results_folder=str(tmp_path))
+    solver = wg.SolverFIT3D(grid, wake, bc_low=["pec"] * 3, bc_high=["pec"] * 3, use_stl=True, bg="pec",
+                            dtype=np.float32, verbose=0)
+    solver.wakesolve(wakelength=1.0)
+    assert solver.Nt == int(z["Nt"])
+    # the reference test's own assertions (tests/test_001_pec_cubic_cavity.py:153-177)
+    assert np.allclose(wake.WP[::50], z["WP_samples"], rtol=50e-6, atol=50e-6)
+    assert np.cumsum(np.abs(wake.WP))[-1] == pytest.approx(float(z["WP_cumsum"]), 0.1)
+    for f in (np.abs, np.real, np.imag):
+        assert np.allclose(f(wake.Z)[::20], f(z["Z_samples"]), rtol=50e-5, atol=50e-5)
+    assert np.cumsum(np.abs(wake.Z))[-1] == pytest.approx(float(z["Z_cumsum"]), 0.1)
+    # and the reference's full run of the same case
+    np.testing.assert_array_equal(wake.s, z["s"])
+    assert rel_l2(wake.WP, z["WP"]) < 1e-4
+    assert rel_l2(wake.Z, z["Z"]) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["config1a", "config1b"])
+def test_config1_fp32_against_fp64(name, tmp_path):
+    case = C.CONFIGS[name]
+    r32 = run_case(name, case=case, tmpdir=tmp_path, dtype=np.float32)
+    r64 = run_case(name, case=dict(case, dtype="float64"), tmpdir=tmp_path, dtype=np.float64)
+    # dt is rounded to the solver dtype (as in the reference), so the s axes differ in the
+    # last bits and possibly by one sample at the end
+    n = min(len(r32["WP"]), len(r64["WP"]))
+    assert np.allclose(r32["s"][:n], r64["s"][:n], rtol=1e-6, atol=1e-9)
+    assert rel_l2(r32["WP"][:n], r64["WP"][:n]) < 1e-4
