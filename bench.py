@@ -94,13 +94,13 @@ class Pillbox:
         vac = ((r2 <= self.R ** 2) & (Z.abs() <= self.L / 2)) | (r2 <= self.rp ** 2)
         return ~vac
 
-    def build(self, wg, mask, dtype=np.float32, results=None):
+    def build(self, wg, mask, dtype=np.float32, results=None, dt=None):
         x, y, z = self.axes()
         grid = wg.GridFIT3D(x=x, y=y, z=z, stl_solids={"walls": mask},
                             stl_materials={"walls": [1.0, 1.0, self.sigma]}, verbose=0)
         wake = wg.WakeSolver(wakelength=self.wakelength, q=1e-9, sigmaz=self.sigmaz, beta=1.0, save=False,
                              verbose=0, results_folder=results or tempfile.mkdtemp())
-        solver = wg.SolverFIT3D(grid, wake, cfln=self.cfln, bc_low=["pec", "pec", "pml"],
+        solver = wg.SolverFIT3D(grid, wake, cfln=self.cfln, dt=dt, bc_low=["pec", "pec", "pml"],
                                 bc_high=["pec", "pec", "pml"], use_stl=True, bg=[1.0, 1.0], dtype=dtype,
                                 n_pml=self.n_pml, verbose=0)
         return grid, wake, solver
@@ -206,8 +206,8 @@ def run_ours(args, rank, world):
     N = P.nx * P.ny * P.nz
     mask = P.walls_mask(device=dev)
     grid, wake, s = P.build(wg, mask)
-    if args.variant == "direct":
-        s._ctx.call("fit_set_kernel_variant", 0)
+    if args.variant == "staged":
+        s._ctx.call("fit_set_kernel_variant", 1)
     del mask
     beam, Nt = s._wake_prepare(wake, P.wakelength, "both")
     vt = s._wake_device_setup(beam, Nt)
@@ -312,7 +312,14 @@ def _rel(a, b, ref=None):
 def run_accuracy(args):
     """FP32 runs against the FP64 CUDA path (validated against the CPU oracle at 1e-10):
     config 1 (both beam runs: fields, WP, WPx, WPy, Z, Zx, Zy), config 2 (64 probes of
-    Ez over 2000 steps) and, with --accuracy-cfg4, config 4 (WP over the first 0.3 m)."""
+    Ez over 2000 steps) and, with --accuracy-cfg4, config 4 (WP over the first 0.3 m).
+
+    An FP32 solver rounds dt to float32, as the reference does.  The main comparison
+    ("same_dt") runs FP64 at that rounded dt, so it isolates field precision.  The second
+    ("cfl_dt") runs FP64 at its own CFL step.  Its gap adds the post-processor's
+    sensitivity to dt: the wake time index int(.../dt) flips for some (s, z) pairs.
+    """
+    import gc
     import torch
     import wakis_gb300 as wg
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -321,35 +328,49 @@ def run_accuracy(args):
     from product_runner import make_grid, make_solver
     out = {}
     tmp = tempfile.mkdtemp()
-    for name in ("config1a", "config1b"):
-        case = CS.CONFIGS[name]
-        res = {}
-        for dt in (np.float32, np.float64):
-            grid = make_grid(wg, case)
-            wake = wg.WakeSolver(wakelength=case["wakelength"], save=False, verbose=0, results_folder=tmp,
-                                 **case["wake"])
-            s = make_solver(wg, case, grid, wake, dt)
-            t0 = time.perf_counter()
-            s.wakesolve(wakelength=case["wakelength"])
-            torch.cuda.synchronize()
-            res[dt] = dict(sec=time.perf_counter() - t0, Nt=s.Nt, s=wake.s, WP=wake.WP, WPx=wake.WPx, WPy=wake.WPy,
-                           Z=wake.Z, Zx=wake.Zx, Zy=wake.Zy, E=s.E.numpy(), H=s.H.numpy())
-            del s, grid, wake
-        a, b = res[np.float32], res[np.float64]
+
+    def free():
+        gc.collect()
+        torch.cuda.empty_cache()
+
+    def wake_run(case, dtype, dt=None):
+        grid = make_grid(wg, case)
+        wake = wg.WakeSolver(wakelength=case["wakelength"], save=False, verbose=0, results_folder=tmp,
+                             **case["wake"])
+        s = make_solver(wg, case, grid, wake, dtype, dt)
+        t0 = time.perf_counter()
+        s.wakesolve(wakelength=case["wakelength"])
+        torch.cuda.synchronize()
+        r = dict(sec=time.perf_counter() - t0, Nt=s.Nt, dt=float(s.dt), s=wake.s, WP=wake.WP, WPx=wake.WPx,
+                 WPy=wake.WPy, Z=wake.Z, Zx=wake.Zx, Zy=wake.Zy, E=s.E.numpy(), H=s.H.numpy())
+        del s, grid, wake
+        free()
+        return r
+
+    def wake_err(a, b):
         n = min(len(a["WP"]), len(b["WP"]))
         m = min(len(a["Z"]), len(b["Z"]))
-        out[name] = {"Nt_fp32": a["Nt"], "Nt_fp64": b["Nt"], "seconds_fp32": a["sec"], "seconds_fp64": b["sec"],
-                     "WP": _rel(a["WP"][:n], b["WP"][:n]), "WPx": _rel(a["WPx"][:n], b["WPx"][:n], b["WP"][:n]),
-                     "WPy": _rel(a["WPy"][:n], b["WPy"][:n], b["WP"][:n]), "Z": _rel(a["Z"][:m], b["Z"][:m]),
-                     "Zx": _rel(a["Zx"][:m], b["Zx"][:m], b["Z"][:m]), "Zy": _rel(a["Zy"][:m], b["Zy"][:m], b["Z"][:m]),
-                     "E": _rel(a["E"], b["E"]), "H": _rel(a["H"], b["H"])}
+        return {"WP": _rel(a["WP"][:n], b["WP"][:n]), "WPx": _rel(a["WPx"][:n], b["WPx"][:n], b["WP"][:n]),
+                "WPy": _rel(a["WPy"][:n], b["WPy"][:n], b["WP"][:n]), "Z": _rel(a["Z"][:m], b["Z"][:m]),
+                "Zx": _rel(a["Zx"][:m], b["Zx"][:m], b["Z"][:m]), "Zy": _rel(a["Zy"][:m], b["Zy"][:m], b["Z"][:m]),
+                "E": _rel(a["E"], b["E"]), "H": _rel(a["H"], b["H"]), "Nt": [a["Nt"], b["Nt"]]}
+
+    for name in ("config1a", "config1b"):
+        case = CS.CONFIGS[name]
+        a = wake_run(case, np.float32)
+        b = wake_run(case, np.float64, a["dt"])
+        c = wake_run(case, np.float64)
+        out[name] = {"same_dt": wake_err(a, b), "cfl_dt": wake_err(a, c), "dt_fp32": a["dt"], "dt_fp64": c["dt"],
+                     "seconds_fp32": a["sec"], "seconds_fp64": b["sec"]}
     # config 2: probes
     case = CS.CONFIGS["config2"]
     P = CS.probe_points(case)
     probes = {}
-    for dt in (np.float32, np.float64):
+    dt32 = None
+    for key, dtype in (("fp32", np.float32), ("fp64", np.float64)):
         grid = make_grid(wg, case)
-        s = make_solver(wg, case, grid, dtype=dt)
+        s = make_solver(wg, case, grid, dtype=dtype, dt=dt32)
+        dt32 = float(s.dt)
         sc = case["source"]
         src = wg.sources.WavePacket(zs=sc["zs"], sigmaz=sc["sigmaz"], sigmaxy=sc["sigmaxy"],
                                     wavelength=sc["wavelength"], amplitude=sc["amplitude"])
@@ -358,31 +379,33 @@ def run_accuracy(args):
         t0 = time.perf_counter()
         s.emsolve(case["Nt"], source=src, callback=lambda sv, t: rec.append(sv.E.array[flat].double()))
         torch.cuda.synchronize()
-        probes[dt] = (torch.stack(rec).cpu().numpy(), time.perf_counter() - t0)
+        probes[key] = (torch.stack(rec).cpu().numpy(), time.perf_counter() - t0)
         del s, grid
-    out["config2"] = {"probe_Ez_rel_l2": _rel(probes[np.float32][0], probes[np.float64][0]),
-                      "probe_Ez_max_abs_over_max": float(np.abs(probes[np.float32][0] - probes[np.float64][0]).max()
-                                                         / np.abs(probes[np.float64][0]).max()),
-                      "steps": case["Nt"], "probes": int(len(P))}
+        free()
+    a, b = probes["fp32"][0], probes["fp64"][0]
+    out["config2"] = {"probe_Ez_rel_l2": _rel(a, b), "probe_Ez_max_abs_over_max": float(np.abs(a - b).max()
+                                                                                        / np.abs(b).max()),
+                      "steps": case["Nt"], "probes": int(len(P)), "dt": "FP64 run at the FP32 run's dt",
+                      "seconds_fp32": probes["fp32"][1], "seconds_fp64": probes["fp64"][1]}
     if args.accuracy_cfg4:
         P4 = Pillbox()
         res = {}
-        for dt in (np.float32, np.float64):
+        dt32 = None
+        for key, dtype in (("fp32", np.float32), ("fp64", np.float64)):
             mask = P4.walls_mask(device=torch.device("cuda", 0))
-            grid, wake, s = P4.build(wg, mask, dtype=dt)
+            grid, wake, s = P4.build(wg, mask, dtype=dtype, dt=dt32)
+            dt32 = float(s.dt)
             del mask
             t0 = time.perf_counter()
             s.wakesolve(wakelength=P4.wakelength)
             torch.cuda.synchronize()
-            res[dt] = dict(sec=time.perf_counter() - t0, s=wake.s, WP=wake.WP, Z=wake.Z, Nt=s.Nt)
+            res[key] = dict(sec=time.perf_counter() - t0, s=wake.s, WP=wake.WP, Z=wake.Z, Nt=s.Nt)
             del s, grid, wake
-            import gc
-            gc.collect()
-            torch.cuda.empty_cache()
-        a, b = res[np.float32], res[np.float64]
-        n = min(len(a["WP"]), len(b["WP"]))
-        out["config4"] = {"WP_first_0.3m": _rel(a["WP"][:n], b["WP"][:n]), "Z": _rel(a["Z"], b["Z"]),
-                          "Nt": a["Nt"], "seconds_fp32": a["sec"], "seconds_fp64": b["sec"]}
+            free()
+        a, b = res["fp32"], res["fp64"]
+        out["config4"] = {"WP_first_0.3m": _rel(a["WP"], b["WP"]), "Z": _rel(a["Z"], b["Z"]),
+                          "Nt": [a["Nt"], b["Nt"]], "dt": "FP64 run at the FP32 run's dt",
+                          "seconds_fp32": a["sec"], "seconds_fp64": b["sec"]}
     print(json.dumps({"accuracy": out}), flush=True)
 
 
@@ -411,8 +434,8 @@ def main():
     ap.add_argument("--grid", type=int, nargs=3, default=None)
     ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 errors on configs 1, 2 (and 4)")
     ap.add_argument("--accuracy-cfg4", action="store_true")
-    ap.add_argument("--variant", default="staged", choices=["staged", "direct"],
-                    help="pass kernels: persistent bulk-copy staged kernels or direct-load kernels")
+    ap.add_argument("--variant", default="direct", choices=["staged", "direct"],
+                    help="pass kernels: direct-load kernels (default) or the persistent bulk-copy staged kernels")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -20,14 +20,14 @@ def make_grid(wg, case):
                         verbose=0, **kw)
 
 
-def make_solver(wg, case, grid, wake=None, dtype=None):
-    dt = dtype or (np.float32 if case["dtype"] == "float32" else np.float64)
-    return wg.SolverFIT3D(grid, wake, cfln=case.get("cfln", 0.5), bc_low=list(case["bc_low"]),
-                          bc_high=list(case["bc_high"]), use_stl=bool(case.get("solids")), bg=case["bg"], dtype=dt,
+def make_solver(wg, case, grid, wake=None, dtype=None, dt=None):
+    dty = dtype or (np.float32 if case["dtype"] == "float32" else np.float64)
+    return wg.SolverFIT3D(grid, wake, cfln=case.get("cfln", 0.5), dt=dt, bc_low=list(case["bc_low"]),
+                          bc_high=list(case["bc_high"]), use_stl=bool(case.get("solids")), bg=case["bg"], dtype=dty,
                           n_pml=case.get("n_pml", 10), verbose=0)
 
 
-def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None):
+def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None, dt=None):
     import wakis_gb300 as wg
     case = case or C.CASES[name]
     kind = case["kind"]
@@ -50,7 +50,7 @@ def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None):
     if kind == "wake":
         wake = wg.WakeSolver(wakelength=case["wakelength"], save=False, verbose=0, results_folder=str(tmpdir),
                              **case["wake"])
-        s = make_solver(wg, case, grid, wake, dtype)
+        s = make_solver(wg, case, grid, wake, dtype, dt)
         s.logger.wakeSolver["results_folder"] = str(tmpdir)
         s.wakesolve(wakelength=case["wakelength"], compute_plane=case["compute_plane"])
         res = dict(Nt=s.Nt, dt=np.float64(s.dt), s=wake.s, WP=wake.WP, f=wake.f, Z=wake.Z, lambdas=wake.lambdas,
@@ -58,7 +58,7 @@ def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None):
         if case["compute_plane"] != "longitudinal":
             res.update(WP_3d=wake.WP_3d, WPx=wake.WPx, WPy=wake.WPy, Zx=wake.Zx, Zy=wake.Zy)
         return res
-    s = make_solver(wg, case, grid, dtype=dtype)
+    s = make_solver(wg, case, grid, dtype=dtype, dt=dt)
     if kind == "userloop":
         beam = wg.sources.Beam(**case["beam"])
         for n in range(case["Nt"]):

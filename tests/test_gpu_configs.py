@@ -69,11 +69,15 @@ def test_reference_test001_goldens_on_gpu(tmp_path):
 
 @pytest.mark.parametrize("name", ["config1a", "config1b"])
 def test_config1_fp32_against_fp64(name, tmp_path):
+    """FP32 fields against FP64 fields at the same time step.  An FP32 solver rounds dt
+    to float32 (as the reference does); run at the FP64 CFL step instead, the wake's time
+    index int(.../dt) flips for some (s, z) pairs and moves WP near the bunch by ~1e-3
+    -- a sampling effect of the post-processor, not of the field precision -- so the
+    FP64 run is given the FP32 run's dt."""
     case = C.CONFIGS[name]
     r32 = run_case(name, case=case, tmpdir=tmp_path, dtype=np.float32)
-    r64 = run_case(name, case=dict(case, dtype="float64"), tmpdir=tmp_path, dtype=np.float64)
-    # dt is rounded to the solver dtype (as in the reference), so the s axes differ in the
-    # last bits and possibly by one sample at the end
-    n = min(len(r32["WP"]), len(r64["WP"]))
-    assert np.allclose(r32["s"][:n], r64["s"][:n], rtol=1e-6, atol=1e-9)
-    assert rel_l2(r32["WP"][:n], r64["WP"][:n]) < 1e-4
+    r64 = run_case(name, case=dict(case, dtype="float64"), tmpdir=tmp_path, dtype=np.float64, dt=float(r32["dt"]))
+    assert int(r32["Nt"]) == int(r64["Nt"])
+    np.testing.assert_array_equal(r32["s"], r64["s"])
+    assert rel_l2(r32["WP"], r64["WP"]) < 1e-4
+    assert rel_l2(r32["Z"], r64["Z"]) < 1e-4

@@ -26,7 +26,7 @@ def test_oracle_matches_reference(name):
             np.testing.assert_array_equal(o[k], v)
         else:
             assert np.shape(o[k]) == np.shape(v), k
-            scale = max(float(np.linalg.norm(np.asarray(v, dtype=np.float64))), 1e-300)
+            scale = max(float(np.linalg.norm(np.asarray(v, dtype=np.complex128))), 1e-300)
             if k in ("WPx", "WPy", "Zx", "Zy"):
                 # transverse wakes of symmetric cases are ~0: compare on the scale of WP / Z
                 ref = g["WP"] if k.startswith("WP") else g["Z"]
