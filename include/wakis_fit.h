@@ -37,6 +37,7 @@ extern "C" {
 #define FIT_ERR_TIMEOUT (-4)
 #define FIT_ERR_NOMEM (-5)
 #define FIT_ERR_DEVICE (-6)
+#define FIT_ERR_BUDGET (-7) /* a pool reservation would exceed the pool's memory budget */
 
 #define FIT_F32 0
 #define FIT_F64 1
@@ -198,14 +199,78 @@ FIT_API int fit_dft_noalloc(const double *x, int32_t nsig, int64_t len, int64_t 
  * then returned without completing its pass).  The word is cleared by the read. */
 FIT_API int fit_check_error(FitCtx *ctx);
 
-/* Chooses the pass kernels: staged != 0 (default) uses the persistent bulk-copy kernels
- * when Nx*sizeof(dtype) is a multiple of 16 bytes; 0 always uses the direct kernels. */
+/* Chooses the pass kernels: staged != 0 uses the persistent bulk-copy kernels when
+ * Nx*sizeof(dtype) is a multiple of 16 bytes; 0 (the default) uses the direct kernels. */
 FIT_API int fit_set_kernel_variant(FitCtx *ctx, int32_t staged);
 
 /* Benchmark support: launches the H pass reps times, then the elided-J E pass reps
  * times (advancing the fields), on the context's stream between CUDA events; ms_out
  * (host, 2 values) receives the average milliseconds per launch of each kernel. */
 FIT_API int fit_time_kernels(FitCtx *ctx, int32_t reps, double *ms_out);
+
+/* ---------------------------------------------------------------- serving pool
+ * No counterpart in the reference: Wakis runs one solve per process, each wakesolve
+ * (wakis/routines.py:231-485) stepping its own grid.  A pool advances many independent
+ * FP32 contexts (grids of any size) together on one GPU: every step is three launches
+ * that cover all member grids (wake taps + step counters, H pass, E pass), driven by a
+ * device work table with one row per context and replayed from CUDA graphs in chunks of
+ * chunk_steps steps.  A native driver thread runs the chunks (two in flight), retires
+ * contexts whose steps are done and admits newly submitted ones at the next chunk, so
+ * solves join and leave while others run (continuous batching).  Each context's fields,
+ * wake sums and step counter evolve exactly as under fit_run: the per-cell arithmetic
+ * is the same code.
+ *
+ * Memory admission: fit_pool_reserve / fit_pool_release keep a byte count against the
+ * pool's budget; a caller reserves a solve's footprint before allocating it and
+ * releases it after freeing it.  The pool never allocates field storage itself. */
+typedef struct FitPool FitPool;
+
+typedef struct FitPoolDone {
+    int64_t tag;       /* the tag given to fit_pool_submit */
+    int64_t steps;     /* steps taken */
+    int32_t status;    /* FIT_OK, or the error that stopped the pool */
+    int32_t reserved;
+    double t_submit_ms; /* host times in ms since fit_pool_create: submitted, */
+    double t_start_ms;  /* first chunk containing the context launched, */
+    double t_done_ms;   /* completion of its last chunk observed */
+} FitPoolDone;
+
+typedef struct FitPoolStats {
+    int64_t chunks;         /* graph replays */
+    int64_t cell_updates;   /* sum over contexts of N * steps taken */
+    int64_t budget_bytes, reserved_bytes;
+    int32_t active;         /* contexts in the work table or in flight */
+    int32_t queued;         /* submitted, waiting for a table row */
+    int32_t max_active;     /* most contexts stepped by one chunk */
+    int32_t grid_h, grid_e; /* persistent CTAs of the pooled H and E passes */
+    int32_t chunk_steps;
+    double busy_ms;         /* host time with at least one chunk in flight */
+} FitPoolStats;
+
+/* device: CUDA ordinal; budget_bytes > 0; chunk_steps in [1, 1024] (64 is a good
+ * default); ctas_per_sm: persistent CTAs per SM of the pass kernels, 0 = as many as
+ * the kernels' occupancy allows.  Starts the driver thread. */
+FIT_API int fit_pool_create(int32_t device, int64_t budget_bytes, int32_t chunk_steps, int32_t ctas_per_sm,
+                            FitPool **out);
+/* Stops the driver after the chunks in flight; contexts still in the pool are
+ * reported with status FIT_ERR_STATE and become usable again. */
+FIT_API int fit_pool_destroy(FitPool *pool);
+FIT_API int fit_pool_last_error(const FitPool *pool, char *buf, int64_t len);
+/* FIT_OK, FIT_ERR_BUDGET (retry after a release), or FIT_ERR_ARG when bytes exceeds
+ * the whole budget. */
+FIT_API int fit_pool_reserve(FitPool *pool, int64_t bytes);
+FIT_API int fit_pool_release(FitPool *pool, int64_t bytes);
+/* Hands a ready FP32 context to the pool for steps n0 .. n0+nsteps-1, as fit_run(ctx,
+ * n0, nsteps) would take them (elided J, beam from the v*t table, wake taps).  Work
+ * queued on the context's streams before the call is ordered before its first pooled
+ * step.  Until the pool reports the tag done, every other call on ctx fails with
+ * FIT_ERR_STATE.  Contexts with a plane source or low-face ABC updates (emsolve
+ * features) are rejected. */
+FIT_API int fit_pool_submit(FitPool *pool, FitCtx *ctx, int64_t n0, int64_t nsteps, int64_t tag);
+/* Copies up to max finished solves into out and returns how many (>= 0), waiting up to
+ * wait_ms for the first one when none is ready and work is pending. */
+FIT_API int fit_pool_poll(FitPool *pool, FitPoolDone *out, int32_t max, int32_t wait_ms);
+FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
 
 /* Library build information: sm architecture compiled for, and the kernel launch
  * counter (kernels issued since load), for bench accounting. */

@@ -1,0 +1,140 @@
+"""Serving pool on the GPU: pooled solves give the same results as the plain public API
+(bit for bit: the per-cell arithmetic is the same code), alone or in a mix, under a
+budget that admits one at a time or all at once; contexts are locked while pooled."""
+
+import numpy as np
+import pytest
+import torch
+
+import wakis_gb300._native as nat
+from wakis_gb300 import serving as S
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("s", "WP", "WPx", "WPy", "f", "Z", "Zx", "Zy")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def small_requests():
+    # Nx = 16, 18, 21: vector widths 4, 2 and 1 in the pooled passes; PEC and lossy walls
+    return [S.CavityRequest(tag=0, side=20e-3, rp=4e-3, n=16, sigmaz=6e-3, sigma=0.0, wakelength=0.06),
+            S.CavityRequest(tag=1, side=24e-3, rp=5e-3, n=18, sigmaz=7e-3, sigma=2e4, wakelength=0.05),
+            S.CavityRequest(tag=2, side=22e-3, rp=3e-3, n=21, sigmaz=5e-3, sigma=0.0, wakelength=0.04),
+            S.CavityRequest(tag=3, side=30e-3, rp=6e-3, n=24, sigmaz=8e-3, sigma=5e5, wakelength=0.05)]
+
+
+@pytest.fixture(scope="module")
+def alone():
+    return {r.tag: S.solve_alone(r, np.float32) for r in small_requests()}
+
+
+def assert_same(got, ref):
+    for k in KEYS:
+        np.testing.assert_array_equal(np.asarray(got[k]), np.asarray(ref[k]), err_msg=k)
+
+
+def test_pooled_mix_matches_wakesolve(alone):
+    loop = S.ServingLoop(budget_bytes=8 << 30, chunk_steps=16)
+    try:
+        recs, summ = loop.run(small_requests())
+    finally:
+        loop.close()
+    assert summ["solves"] == 4
+    for tag, ref in alone.items():
+        assert_same(loop.results[tag], ref)
+    assert {r["tag"]: r["steps"] for r in recs} == {t: alone[t]["Nt"] for t in alone}
+
+
+def test_solves_submitted_together_share_chunks(alone):
+    """All solves built first, then submitted back to back: they run in the same chunks."""
+    jobs = [S.ServedSolve(r) for r in small_requests()]
+    pool = nat.Pool(8 << 30, chunk_steps=8)
+    try:
+        for j in jobs:
+            j.submit(pool)
+        done = []
+        while len(done) < len(jobs):
+            done += pool.poll(wait_ms=200)
+        st = pool.stats()
+    finally:
+        pool.close()
+    assert all(d["status"] == 0 for d in done)
+    assert st["max_active"] >= 2
+    assert st["cell_updates"] == sum(j.req.cells * (j.Nt - j.first) for j in jobs)
+    for j in jobs:
+        assert_same(j.finish(), alone[j.req.tag])
+        j.close()
+
+
+def test_one_at_a_time_budget_gives_the_same_results(alone):
+    reqs = small_requests()
+    biggest = max(S.footprint_bytes(r) for r in reqs)
+    loop = S.ServingLoop(budget_bytes=biggest, chunk_steps=64)
+    try:
+        recs, summ = loop.run(reqs)
+    finally:
+        loop.close()
+    assert summ["pool"]["max_active"] == 1
+    assert summ["pool"]["reserved_bytes"] == 0
+    for tag, ref in alone.items():
+        assert_same(loop.results[tag], ref)
+
+
+def test_staggered_arrivals_join_running_solves(alone):
+    reqs = small_requests()
+    for i, r in enumerate(reqs):
+        r.arrival = 0.02 * i
+    loop = S.ServingLoop(budget_bytes=8 << 30, chunk_steps=4)
+    try:
+        recs, summ = loop.run(reqs)
+    finally:
+        loop.close()
+    for tag, ref in alone.items():
+        assert_same(loop.results[tag], ref)
+    assert all(r["tti_s"] >= 0 for r in recs)
+
+
+def test_context_is_locked_while_pooled():
+    req = S.CavityRequest(tag=7, side=40e-3, rp=5e-3, n=64, sigmaz=6e-3, sigma=0.0, wakelength=1.0)
+    pool = nat.Pool(8 << 30, chunk_steps=64)
+    job = S.ServedSolve(req)
+    try:
+        job.submit(pool)
+        with pytest.raises(nat.FitError) as e:
+            job.solver._ctx.call("fit_zero_ghosts")
+        assert e.value.code == -3
+        with pytest.raises(nat.FitError):
+            job.submit(pool)
+        done = []
+        while not done:
+            done = pool.poll(wait_ms=200)
+        assert done[0]["tag"] == 7 and done[0]["status"] == 0 and done[0]["steps"] == job.Nt - job.first
+        job.solver._ctx.call("fit_check_error")  # usable again
+        res = job.finish()
+        assert np.isfinite(res["WP"]).all()
+    finally:
+        pool.close()
+        job.close()
+
+
+def test_pool_rejects_fp64_contexts():
+    req = S.CavityRequest(tag=0, side=20e-3, rp=4e-3, n=16, sigmaz=6e-3, sigma=0.0, wakelength=0.05)
+    pool = nat.Pool(1 << 30)
+    job = S.ServedSolve(req, dtype=np.float64)
+    try:
+        with pytest.raises(nat.FitError) as e:
+            job.submit(pool)
+        assert e.value.code == -1
+        with pytest.raises(nat.FitError):
+            pool.reserve(4 << 30)  # larger than the whole budget
+        assert pool.reserve(1 << 29)
+        assert not pool.reserve(1 << 30)
+        pool.release(1 << 29)
+    finally:
+        pool.close()
+        job.close()

@@ -16,8 +16,9 @@ FIT_F32, FIT_F64 = 0, 1
 FIT_BC = {"periodic": 0, "pec": 1, "electric": 1, "pml": 2, "pmc": 3, "magnetic": 3, "abc": 4}
 FIT_J_ELIDED, FIT_J_EXPLICIT = 0, 1
 
+FIT_ERR_BUDGET = -7
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "invalid state", -4: "timeout", -5: "out of memory",
-           -6: "no device"}
+           -6: "no device", -7: "over the pool budget"}
 
 
 class FitError(RuntimeError):
@@ -33,6 +34,18 @@ class FitGridDesc(C.Structure):
                 ("use_conductivity", C.c_int32), ("bc_lo", C.c_int32 * 3), ("bc_hi", C.c_int32 * 3),
                 ("device", C.c_int32), ("reserved", C.c_int32), ("E", C.c_void_p), ("H", C.c_void_p),
                 ("J", C.c_void_p)]
+
+
+class FitPoolDone(C.Structure):
+    _fields_ = [("tag", C.c_int64), ("steps", C.c_int64), ("status", C.c_int32), ("reserved", C.c_int32),
+                ("t_submit_ms", C.c_double), ("t_start_ms", C.c_double), ("t_done_ms", C.c_double)]
+
+
+class FitPoolStats(C.Structure):
+    _fields_ = [("chunks", C.c_int64), ("cell_updates", C.c_int64), ("budget_bytes", C.c_int64),
+                ("reserved_bytes", C.c_int64), ("active", C.c_int32), ("queued", C.c_int32),
+                ("max_active", C.c_int32), ("grid_h", C.c_int32), ("grid_e", C.c_int32),
+                ("chunk_steps", C.c_int32), ("busy_ms", C.c_double)]
 
 
 _P = C.c_void_p
@@ -70,6 +83,14 @@ _SIGS = {
     "fit_check_error": (_P,),
     "fit_dft_noalloc": (_P, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P, _P),
     "fit_set_kernel_variant": (_P, C.c_int32),
+    "fit_pool_create": (C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)),
+    "fit_pool_destroy": (_P,),
+    "fit_pool_last_error": (_P, C.c_char_p, C.c_int64),
+    "fit_pool_reserve": (_P, C.c_int64),
+    "fit_pool_release": (_P, C.c_int64),
+    "fit_pool_submit": (_P, _P, C.c_int64, C.c_int64, C.c_int64),
+    "fit_pool_poll": (_P, C.POINTER(FitPoolDone), C.c_int32, C.c_int32),
+    "fit_pool_stats": (_P, C.POINTER(FitPoolStats)),
     "fit_version": (C.c_char_p, C.c_int64),
     "fit_launch_count": (),
 }
@@ -173,6 +194,67 @@ class Context:
     def close(self):
         if getattr(self, "h", None):
             self.lib.fit_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Pool:
+    """Owns one FitPool (the serving executor of FP32 wake solves on one device)."""
+
+    def __init__(self, budget_bytes, chunk_steps=64, ctas_per_sm=0, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.fit_pool_create(int(device), int(budget_bytes), int(chunk_steps), int(ctas_per_sm),
+                                      C.byref(h))
+        if rc != 0:
+            raise FitError(rc, self._err(None))
+        self.h = h
+
+    def _err(self, h):
+        buf = C.create_string_buffer(1024)
+        self.lib.fit_pool_last_error(h, buf, len(buf))
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc):
+        if rc < 0:
+            raise FitError(rc, self._err(self.h))
+        return rc
+
+    def reserve(self, nbytes):
+        """True when nbytes fit in the budget now (and are reserved), False otherwise."""
+        rc = self.lib.fit_pool_reserve(self.h, int(nbytes))
+        if rc == FIT_ERR_BUDGET:
+            return False
+        self._check(rc)
+        return True
+
+    def release(self, nbytes):
+        self._check(self.lib.fit_pool_release(self.h, int(nbytes)))
+
+    def submit(self, ctx, n0, nsteps, tag):
+        rc = self.lib.fit_pool_submit(self.h, ctx.h, int(n0), int(nsteps), int(tag))
+        if rc != 0:
+            raise FitError(rc, last_error(ctx.h))
+
+    def poll(self, wait_ms=0, max_n=64):
+        out = (FitPoolDone * max_n)()
+        n = self._check(self.lib.fit_pool_poll(self.h, out, max_n, int(wait_ms)))
+        return [dict(tag=d.tag, steps=d.steps, status=d.status, t_submit_ms=d.t_submit_ms,
+                     t_start_ms=d.t_start_ms, t_done_ms=d.t_done_ms) for d in out[:n]]
+
+    def stats(self):
+        s = FitPoolStats()
+        self._check(self.lib.fit_pool_stats(self.h, C.byref(s)))
+        return {name: getattr(s, name) for name, _ in FitPoolStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fit_pool_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -84,6 +84,7 @@ struct FitCtx {
     int* d_err = nullptr;   // device error word written by kernels (FIT_ERR_TIMEOUT)
     int nsm = 1;            // SM count: grid of the persistent staged kernels
     bool staged = false;    // staged (bulk-copy) passes when the grid is aligned (opt-in)
+    std::atomic<bool> in_pool{false};  // submitted to a FitPool and not yet reported done
     std::string err;
 };
 
@@ -142,6 +143,7 @@ void dfree(void* p) {
 
 // ordering with the caller's stream
 int enter(FitCtx* c) {
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     CK(cudaSetDevice(c->device));
     CK(cudaEventRecord(c->ev_in, c->user));
     CK(cudaStreamWaitEvent(c->own, c->ev_in, 0));
@@ -404,6 +406,7 @@ int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
 
 int fit_ctx_destroy(FitCtx* c) {
     if (!c) return FIT_OK;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     cudaSetDevice(c->device);
     if (c->own) cudaStreamSynchronize(c->own);
     if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -442,12 +445,14 @@ int fit_last_error(const FitCtx* c, char* buf, int64_t len) {
 
 int fit_set_stream(FitCtx* c, void* stream) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     c->user = static_cast<cudaStream_t>(stream);
     return FIT_OK;
 }
 
 int fit_set_fields(FitCtx* c, void* E, void* H, void* J) {
     if (!c || !E || !H || !J) return fail(c, FIT_ERR_ARG, "null field pointer");
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     invalidate(c);
     c->E = E;
     c->H = H;
@@ -490,6 +495,7 @@ int fit_set_metrics(FitCtx* c, const double* dx, const double* dy, const double*
 
 int fit_enable_explicit_j(FitCtx* c) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     if (c->explicit_ready) return FIT_OK;
     const size_t fb = 3 * (size_t)c->g.N * esize(c);
     int rc = dev_alloc(c, &c->cj, fb);
@@ -553,6 +559,7 @@ int fit_zero_ghosts(FitCtx* c) {
 int fit_set_beam(FitCtx* c, int32_t active, int32_t ixs, int32_t iys, double q, double v, double sigmaz, double s0,
                  double dx_s, double dy_s, const double* z, const double* ieps_line) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     invalidate(c);
     if (!active) {
         c->beam.active = 0;
@@ -590,6 +597,7 @@ int fit_set_beam(FitCtx* c, int32_t active, int32_t ixs, int32_t iys, double q, 
 
 int fit_set_beam_vt(FitCtx* c, double vt) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     c->beam_vt = vt;
     return FIT_OK;
 }
@@ -609,6 +617,7 @@ int fit_set_beam_vt_table(FitCtx* c, const double* vt, int64_t n) {
 int fit_set_plane_source(FitCtx* c, int32_t active, int32_t zs, int32_t x0, int32_t x1, int32_t y0, int32_t y1,
                          const double* prof, const double* c1, const double* c2, const double* gt, int64_t n) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     invalidate(c);
     if (!active) {
         c->plane.active = 0;
@@ -650,6 +659,7 @@ int fit_set_plane_source(FitCtx* c, int32_t active, int32_t zs, int32_t x0, int3
 
 int fit_set_abc(FitCtx* c, int32_t lo_axes) {
     if (!c || lo_axes < 0 || lo_axes > 7) return fail(c, FIT_ERR_ARG, "bad abc axes");
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     const int len[3] = {c->g.nx, c->g.ny, c->g.nz};
     for (int a = 0; a < 3; ++a)
         if ((lo_axes >> a) & 1)
@@ -663,6 +673,7 @@ int fit_set_wake_taps(FitCtx* c, int32_t nlines, const int32_t* lx, const int32_
                       int64_t nsteps, const int64_t* row_ptr, const int32_t* ent_m, const int32_t* ent_k0,
                       const int32_t* ent_cnt, int32_t nz_tap, const double* dz) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     invalidate(c);
     if (nlines <= 0) {
         c->tap.nlines = 0;
@@ -963,6 +974,7 @@ int fit_check_error(FitCtx* c) {
 
 int fit_set_kernel_variant(FitCtx* c, int32_t staged) {
     if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     invalidate(c);
     c->staged = staged != 0;
     return FIT_OK;
@@ -1043,3 +1055,6 @@ extern "C" int fit_dft_noalloc(const double* x, int32_t nsig, int64_t len, int64
     if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "fit_dft_noalloc launch failed: %s", cudaGetErrorString(e));
     return FIT_OK;
 }
+
+// serving pool (continuous batching of FP32 wake solves)
+#include "fit_pool.cuh"

@@ -448,13 +448,10 @@ __device__ __forceinline__ void cell_of(long long n, const Geom& g, int& i0, int
 // ---------------------------------------------------------------- direct kernels
 // One thread per VEC cells, inputs loaded straight from global memory.  Used for grids
 // whose Nx is not a multiple of the 16-byte vector width and for the explicit-J pass.
+// H pass of the VEC cells starting at component-local flat index n
 template <typename T, int VEC>
-__global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __restrict__ H,
-                                               const T* __restrict__ ch, Geom g, Metric<T> mt) {
-    const long long nvec = g.N / VEC;
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nvec) return;
-    const long long n = v * VEC;
+__device__ __forceinline__ void hpass_at(const T* __restrict__ E, T* __restrict__ H, const T* __restrict__ ch,
+                                         const Geom& g, const Metric<T>& mt, long long n) {
     int i0, j, k;
     cell_of(n, g, i0, j, k);
     const T* Ex = E;
@@ -499,20 +496,23 @@ __global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __
     st_v<T, VEC>(H + 2 * g.N + n, hz);
 }
 
+template <typename T, int VEC>
+__global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __restrict__ H,
+                                               const T* __restrict__ ch, Geom g, Metric<T> mt) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.N / VEC) return;
+    hpass_at<T, VEC>(E, H, ch, g, mt, v * VEC);
+}
+
 // MODE 0: E += ce*(C^T ĥ)                       (no conduction current)
 // MODE 1: E = cl*E + ce*(C^T ĥ)                 (J = sigma*E_prev folded into cl)
 // MODE 2: E = E + ce*(C^T ĥ) - cj*J; J = sg*E   (explicit J; J written if conductive)
 // The beam line (ixs, iys, :) of the z component uses the beam current instead of J.
 template <typename T, int VEC, int MODE>
-__global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __restrict__ H,
-                                               const T* __restrict__ ce, const T* __restrict__ cl,
-                                               T* __restrict__ J, const T* __restrict__ cj,
-                                               const T* __restrict__ sg, int use_cond, Geom g,
-                                               Metric<T> mt, BeamArgs b, PlaneArgs pl, StepArgs st) {
-    const long long nvec = g.N / VEC;
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nvec) return;
-    const long long n = v * VEC;
+__device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict__ H, const T* __restrict__ ce,
+                                         const T* __restrict__ cl, T* __restrict__ J, const T* __restrict__ cj,
+                                         const T* __restrict__ sg, int use_cond, const Geom& g, const Metric<T>& mt,
+                                         const BeamArgs& b, const PlaneArgs& pl, const StepArgs& st, long long n) {
     int i0, j, k;
     cell_of(n, g, i0, j, k);
     const T* Hx = H;
@@ -613,6 +613,17 @@ __global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __
     st_v<T, VEC>(E + n, ex);
     st_v<T, VEC>(E + g.N + n, ey);
     st_v<T, VEC>(E + 2 * g.N + n, ez);
+}
+
+template <typename T, int VEC, int MODE>
+__global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __restrict__ H,
+                                               const T* __restrict__ ce, const T* __restrict__ cl,
+                                               T* __restrict__ J, const T* __restrict__ cj,
+                                               const T* __restrict__ sg, int use_cond, Geom g,
+                                               Metric<T> mt, BeamArgs b, PlaneArgs pl, StepArgs st) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.N / VEC) return;
+    epass_at<T, VEC, MODE>(E, H, ce, cl, J, cj, sg, use_cond, g, mt, b, pl, st, v * VEC);
 }
 
 // ---------------------------------------------------------------- staged kernels
@@ -1037,24 +1048,10 @@ __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
     s = t;
 }
 
+// wake taps of E^n: the (s, z) pairs whose time index is step n add Ez*dz to their
+// line's running sum (FP64, compensated).  Called by all threads of one block.
 template <typename T>
-__global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneArgs pl, TapArgs tp,
-                           long long n_arg, long long* d_step) {
-    const long long n = d_step ? *d_step : n_arg;
-    // plane source
-    if (pl.active && n >= 0 && n < pl.len) {
-        const int w = pl.x1 - pl.x0, h = pl.y1 - pl.y0;
-        const double c1 = pl.c1[n], c2 = pl.c2[n], gt = pl.gt[n];
-        for (int t = threadIdx.x; t < w * h; t += blockDim.x) {
-            const int i = pl.x0 + t % w, j = pl.y0 + t / w;
-            const double pv = pl.prof ? pl.prof[t] : 1.0;
-            const long long c = i + g.sy * j + g.sz * pl.zs;
-            if (pl.stash) pl.stash[t] = (double)E[c];
-            H[g.N + c] = (T)__dmul_rn(__dmul_rn(c1, pv), gt);
-            E[c] = (T)__dmul_rn(__dmul_rn(c2, pv), gt);
-        }
-    }
-    // wake taps of E^n
+__device__ __forceinline__ void wake_taps(const T* __restrict__ E, const Geom& g, const TapArgs& tp, long long n) {
     if (tp.nlines > 0 && n >= 0 && n < tp.nsteps) {
         const long long r0 = tp.row_ptr[n], r1 = tp.row_ptr[n + 1];
         const long long cnt = (r1 - r0) * tp.nlines;
@@ -1072,6 +1069,26 @@ __global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneAr
             tp.comp[(long long)l * tp.ns + m] = cc;
         }
     }
+}
+
+template <typename T>
+__global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneArgs pl, TapArgs tp,
+                           long long n_arg, long long* d_step) {
+    const long long n = d_step ? *d_step : n_arg;
+    // plane source
+    if (pl.active && n >= 0 && n < pl.len) {
+        const int w = pl.x1 - pl.x0, h = pl.y1 - pl.y0;
+        const double c1 = pl.c1[n], c2 = pl.c2[n], gt = pl.gt[n];
+        for (int t = threadIdx.x; t < w * h; t += blockDim.x) {
+            const int i = pl.x0 + t % w, j = pl.y0 + t / w;
+            const double pv = pl.prof ? pl.prof[t] : 1.0;
+            const long long c = i + g.sy * j + g.sz * pl.zs;
+            if (pl.stash) pl.stash[t] = (double)E[c];
+            H[g.N + c] = (T)__dmul_rn(__dmul_rn(c1, pv), gt);
+            E[c] = (T)__dmul_rn(__dmul_rn(c2, pv), gt);
+        }
+    }
+    wake_taps<T>(E, g, tp, n);
     if (d_step) {
         __syncthreads();
         if (threadIdx.x == 0) *d_step = n + 1;
@@ -1191,6 +1208,145 @@ __global__ void k_dft_reduce(const double2* __restrict__ part, int nsig, int nb,
         neumaier_add(si, ci, v.y);
     }
     out[idx] = make_double2(sr + cr, si + ci);
+}
+
+// ---------------------------------------------------------------- batched (pool) kernels
+// Independent grids ("instances") advance together: one launch of each pass covers the
+// cells of every instance in a device work table.  The instances' flat index spaces are
+// laid end to end in tiles of kPoolTpb threads x vec cells; tile t belongs to the last
+// instance whose first tile is <= t, so a CTA works on one instance at a time and reads
+// that instance's descriptor from shared memory.  A persistent grid walks the tiles: its
+// size does not depend on the table, so one captured graph serves every mix, and the
+// table can change between graph replays.  Each instance keeps its own device step
+// counter; an instance whose counter has reached its end is skipped, so instances that
+// finish inside a chunk of steps cost one descriptor fetch per tile from then on.  The
+// per-cell arithmetic is hpass_at / epass_at, the code of the single-grid kernels, so a
+// pooled instance gives bit-identical fields to the same grid run alone.
+constexpr int kPoolMaxInst = 64;
+constexpr int kPoolTpb = 256;
+
+template <typename T>
+struct PoolInst {
+    Geom g;
+    Metric<T> mt;
+    T* E;
+    T* H;
+    const T* ch;
+    const T* ce;
+    const T* cl;
+    T* J;
+    BeamArgs beam;
+    TapArgs tap;
+    long long* d_step;  // the instance's step counter, advanced by k_prologue_pool
+    const double* vt_table;
+    long long vt_len;
+    long long n_end;  // steps n < n_end are taken
+    long long tile0;  // first tile of the instance
+    long long nvec;   // N / vec
+    int vec;          // cells per thread: 4, 2 or 1 (Nx % vec == 0)
+    int mode;         // 0: lossless, 1: J = sigma*E folded into the loss factor
+    int use_cond;
+    int pad;
+};
+
+template <typename T>
+struct PoolTable {
+    int ninst;
+    int pad;
+    long long ntiles;
+    PoolInst<T> inst[kPoolMaxInst];
+};
+
+// descriptor of the instance owning tile t into shared memory, and its current step
+template <typename T>
+__device__ __forceinline__ void pool_fetch(const PoolTable<T>* __restrict__ tab, int ninst, long long t,
+                                           PoolInst<T>* si, long long* step) {
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tab->inst[mid].tile0 <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    static_assert(sizeof(PoolInst<T>) % 8 == 0, "descriptor copied in 8-byte words");
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&tab->inst[lo]);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(si);
+    for (int w = threadIdx.x; w < (int)(sizeof(PoolInst<T>) / 8); w += blockDim.x) dst[w] = src[w];
+    if (threadIdx.x == 0) *step = *tab->inst[lo].d_step - 1;  // the prologue already advanced it
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPoolTpb, 2) k_hpass_pool(const PoolTable<T>* __restrict__ tab) {
+    __shared__ PoolInst<T> si;
+    __shared__ long long sn;
+    const int ninst = tab->ninst;
+    const long long ntiles = tab->ntiles;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        pool_fetch<T>(tab, ninst, t, &si, &sn);
+        __syncthreads();
+        const long long v = (t - si.tile0) * kPoolTpb + threadIdx.x;
+        if (sn < si.n_end && v < si.nvec) {
+            if (si.vec == 4) {
+                if constexpr (sizeof(T) == 4) hpass_at<T, 4>(si.E, si.H, si.ch, si.g, si.mt, v * 4);
+            } else if (si.vec == 2) {
+                hpass_at<T, 2>(si.E, si.H, si.ch, si.g, si.mt, v * 2);
+            } else {
+                hpass_at<T, 1>(si.E, si.H, si.ch, si.g, si.mt, v);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int VEC>
+__device__ __forceinline__ void epass_pool_cells(const PoolInst<T>& si, long long n) {
+    StepArgs st{};
+    st.d_step = si.d_step;
+    st.vt_table = si.vt_table;
+    st.vt_len = si.vt_len;
+    const PlaneArgs pl{};
+    if (si.mode == 1)
+        epass_at<T, VEC, 1>(si.E, si.H, si.ce, si.cl, si.J, nullptr, nullptr, si.use_cond, si.g, si.mt, si.beam, pl,
+                            st, n);
+    else
+        epass_at<T, VEC, 0>(si.E, si.H, si.ce, si.cl, si.J, nullptr, nullptr, si.use_cond, si.g, si.mt, si.beam, pl,
+                            st, n);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPoolTpb, 2) k_epass_pool(const PoolTable<T>* __restrict__ tab) {
+    __shared__ PoolInst<T> si;
+    __shared__ long long sn;
+    const int ninst = tab->ninst;
+    const long long ntiles = tab->ntiles;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        pool_fetch<T>(tab, ninst, t, &si, &sn);
+        __syncthreads();
+        const long long v = (t - si.tile0) * kPoolTpb + threadIdx.x;
+        if (sn < si.n_end && v < si.nvec) {
+            if (si.vec == 4) {
+                if constexpr (sizeof(T) == 4) epass_pool_cells<T, 4>(si, v * 4);
+            } else if (si.vec == 2) {
+                epass_pool_cells<T, 2>(si, v * 2);
+            } else {
+                epass_pool_cells<T, 1>(si, v);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// one block per table row: wake taps of E^n and the step counter (advanced past the
+// end too, so the passes of this step see n >= n_end and skip the finished instance)
+template <typename T>
+__global__ void k_prologue_pool(const PoolTable<T>* __restrict__ tab) {
+    if ((int)blockIdx.x >= tab->ninst) return;
+    const PoolInst<T>& d = tab->inst[blockIdx.x];
+    const long long n = *d.d_step;
+    if (n < d.n_end) wake_taps<T>(d.E, d.g, d.tap, n);
+    __syncthreads();
+    if (threadIdx.x == 0) *d.d_step = n + 1;
 }
 
 }  // namespace fit

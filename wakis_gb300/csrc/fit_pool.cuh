@@ -1,0 +1,456 @@
+// fit_pool.cuh -- serving pool: continuous batching of FP32 wake solves on one GPU.
+// Part of the fit_capi.cu translation unit (included at its end; uses its helpers).
+//
+// Threads: the caller's threads call reserve / release / submit / poll / stats; one
+// driver thread per pool launches chunks and retires solves.  Shared state is guarded by
+// FitPool::mu.  The driver is the only thread that issues work on the pool stream.
+//
+// Chunks: chunk k replays graph k&1, which reads device table k&1 (rows = member
+// contexts).  Up to two chunks are in flight; before the table of chunk k+1 is staged
+// into pinned buffer (k+1)&1 the driver has waited for chunk k-1, the last user of that
+// buffer and of its device table.  Which contexts a chunk finishes is known on the host
+// when it is launched (every member takes min(chunk, remaining) steps), so no device
+// state is read back between chunks.
+#include <chrono>
+#include <condition_variable>
+#include <cstddef>
+#include <deque>
+#include <thread>
+
+namespace {
+
+struct PoolSlot {
+    FitCtx* c = nullptr;
+    int64_t tag = 0;
+    long long nsteps = 0;
+    long long sched = 0;  // steps enqueued so far
+    PoolInst<float> row{};
+    long long ntiles = 0;
+    cudaEvent_t ready = nullptr;  // end of the caller's work on the context before submit
+    bool joined = false;          // the pool stream has waited on `ready`
+    double t_submit = 0.0, t_start = -1.0;
+};
+
+struct InFlight {
+    int buf = 0;
+    std::vector<PoolSlot*> finishing;
+    double t_launch = 0.0;
+};
+
+}  // namespace
+
+struct FitPool {
+    int device = 0;
+    int nsm = 1;
+    int chunk = 64;
+    int grid_h = 0, grid_e = 0;
+    cudaStream_t ps = nullptr;
+    cudaEvent_t ev[2]{};
+    PoolTable<float>* d_tab[2]{};
+    PoolTable<float>* h_tab[2]{};
+    cudaGraphExec_t graph[2]{};
+    long long budget = 0, reserved = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<PoolSlot*> incoming;
+    std::vector<PoolSlot*> active;
+    std::deque<FitPoolDone> done;
+    std::thread th;
+    bool stop = false;
+    int status = FIT_OK;
+    std::string err;
+    long long chunks = 0, cell_updates = 0;
+    int max_active = 0;
+    double busy_ms = 0.0;
+    std::chrono::steady_clock::time_point t0;
+
+    double now() const {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+int pool_fail(FitPool* p, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (p) {
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->err = buf;
+    } else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        g_create_error = buf;
+    }
+    return code;
+}
+
+void finish_slot(FitPool* p, PoolSlot* s, int status, double t) {
+    // caller holds p->mu
+    FitPoolDone d{};
+    d.tag = s->tag;
+    d.steps = status == FIT_OK ? s->nsteps : 0;
+    d.status = status;
+    d.t_submit_ms = s->t_submit;
+    d.t_start_ms = s->t_start;
+    d.t_done_ms = t;
+    p->done.push_back(d);
+    if (s->ready) cudaEventDestroy(s->ready);
+    s->c->in_pool = false;
+    delete s;
+}
+
+// stops the pool on a CUDA error: every member and queued context is reported failed
+void pool_abort(FitPool* p, cudaError_t e, const char* what) {
+    std::lock_guard<std::mutex> lk(p->mu);
+    char buf[384];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    p->err = buf;
+    p->status = FIT_ERR_CUDA;
+    const double t = p->now();
+    for (PoolSlot* s : p->active) finish_slot(p, s, FIT_ERR_CUDA, t);
+    p->active.clear();
+    for (PoolSlot* s : p->incoming) finish_slot(p, s, FIT_ERR_CUDA, t);
+    p->incoming.clear();
+    p->cv_done.notify_all();
+}
+
+// fills pinned table `b` with the members that still have steps to enqueue
+int stage_table(FitPool* p, int b, std::vector<PoolSlot*>& members) {
+    PoolTable<float>* t = p->h_tab[b];
+    long long tile = 0;
+    int n = 0;
+    for (PoolSlot* s : members) {
+        PoolInst<float>& r = t->inst[n++];
+        r = s->row;
+        r.tile0 = tile;
+        tile += s->ntiles;
+    }
+    t->ninst = n;
+    t->ntiles = tile;
+    return n;
+}
+
+void pool_main(FitPool* p) {
+    if (cudaSetDevice(p->device) != cudaSuccess) {
+        pool_abort(p, cudaErrorInvalidDevice, "cudaSetDevice");
+        return;
+    }
+    std::deque<InFlight> fl;
+    long long k = 0;
+    double busy_since = -1.0;
+    for (;;) {
+        std::vector<PoolSlot*> members;
+        bool launch = false;
+        {
+            std::unique_lock<std::mutex> lk(p->mu);
+            if (p->stop && fl.empty()) break;
+            if (!p->stop && fl.empty() && p->active.empty() && p->incoming.empty()) {
+                p->cv_work.wait(lk, [p] { return p->stop || !p->incoming.empty(); });
+                continue;
+            }
+            if (!p->stop) {
+                while (!p->incoming.empty() && (int)p->active.size() < kPoolMaxInst) {
+                    p->active.push_back(p->incoming.front());
+                    p->incoming.pop_front();
+                }
+                for (PoolSlot* s : p->active)
+                    if (s->sched < s->nsteps) members.push_back(s);
+                launch = !members.empty() && fl.size() < 2;
+            }
+        }
+        if (launch) {
+            const int b = (int)(k & 1);
+            const int n = stage_table(p, b, members);
+            cudaError_t e = cudaSuccess;
+            for (PoolSlot* s : members)
+                if (!s->joined && e == cudaSuccess) {
+                    e = cudaStreamWaitEvent(p->ps, s->ready, 0);
+                    s->joined = true;
+                }
+            const size_t bytes = offsetof(PoolTable<float>, inst) + (size_t)n * sizeof(PoolInst<float>);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_tab[b], p->h_tab[b], bytes, cudaMemcpyHostToDevice, p->ps);
+            if (e == cudaSuccess) e = cudaGraphLaunch(p->graph[b], p->ps);
+            if (e == cudaSuccess) e = cudaEventRecord(p->ev[b], p->ps);
+            if (e != cudaSuccess) {
+                pool_abort(p, e, "pool chunk launch");
+                break;
+            }
+            g_launches += 3LL * p->chunk;
+            InFlight f;
+            f.buf = b;
+            f.t_launch = p->now();
+            if (busy_since < 0) busy_since = f.t_launch;
+            long long cells = 0;
+            for (PoolSlot* s : members) {
+                const long long take = std::min<long long>(p->chunk, s->nsteps - s->sched);
+                if (s->t_start < 0) s->t_start = f.t_launch;
+                s->sched += take;
+                cells += take * s->c->g.N;
+                if (s->sched >= s->nsteps) f.finishing.push_back(s);
+            }
+            {
+                std::lock_guard<std::mutex> lk(p->mu);
+                p->chunks++;
+                p->cell_updates += cells;
+                p->max_active = std::max(p->max_active, n);
+            }
+            fl.push_back(std::move(f));
+            ++k;
+            continue;
+        }
+        // wait for the oldest chunk in flight
+        InFlight f = std::move(fl.front());
+        fl.pop_front();
+        cudaError_t e = cudaEventSynchronize(p->ev[f.buf]);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            pool_abort(p, e, "pool chunk");
+            break;
+        }
+        const double t = p->now();
+        std::lock_guard<std::mutex> lk(p->mu);
+        if (fl.empty()) {
+            p->busy_ms += t - busy_since;
+            busy_since = -1.0;
+        }
+        for (PoolSlot* s : f.finishing) {
+            p->active.erase(std::remove(p->active.begin(), p->active.end(), s), p->active.end());
+            finish_slot(p, s, FIT_OK, t);
+        }
+        if (!f.finishing.empty()) p->cv_done.notify_all();
+    }
+    // stopping: what is still in the pool is handed back unfinished
+    std::lock_guard<std::mutex> lk(p->mu);
+    const double t = p->now();
+    for (PoolSlot* s : p->active) finish_slot(p, s, FIT_ERR_STATE, t);
+    p->active.clear();
+    for (PoolSlot* s : p->incoming) finish_slot(p, s, FIT_ERR_STATE, t);
+    p->incoming.clear();
+    p->cv_done.notify_all();
+}
+
+void pool_free(FitPool* p) {
+    cudaSetDevice(p->device);
+    if (p->ps) cudaStreamSynchronize(p->ps);
+    for (int b = 0; b < 2; ++b) {
+        if (p->graph[b]) cudaGraphExecDestroy(p->graph[b]);
+        if (p->ev[b]) cudaEventDestroy(p->ev[b]);
+        if (p->d_tab[b]) cudaFree(p->d_tab[b]);
+        if (p->h_tab[b]) cudaFreeHost(p->h_tab[b]);
+    }
+    if (p->ps) cudaStreamDestroy(p->ps);
+    delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fit_pool_create(int32_t device, int64_t budget_bytes, int32_t chunk_steps, int32_t ctas_per_sm, FitPool** out) {
+    if (!out) return pool_fail(nullptr, FIT_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (budget_bytes <= 0) return pool_fail(nullptr, FIT_ERR_ARG, "budget_bytes must be > 0");
+    if (chunk_steps < 1 || chunk_steps > 1024) return pool_fail(nullptr, FIT_ERR_ARG, "chunk_steps must be in [1, 1024]");
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) return pool_fail(nullptr, FIT_ERR_ARG, "ctas_per_sm must be in [0, 32]");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return pool_fail(nullptr, FIT_ERR_DEVICE, "no CUDA device available");
+    if (device < 0 || device >= ndev) return pool_fail(nullptr, FIT_ERR_ARG, "invalid device %d", device);
+    FitPool* p = new FitPool();
+    p->device = device;
+    p->budget = budget_bytes;
+    p->chunk = chunk_steps;
+    p->t0 = std::chrono::steady_clock::now();
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, device);
+    int occ_h = 0, occ_e = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_h, k_hpass_pool<float>, kPoolTpb, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_epass_pool<float>, kPoolTpb, 0);
+    if (e == cudaSuccess) {
+        const int ch = ctas_per_sm ? std::min(ctas_per_sm, std::max(occ_h, 1)) : std::max(occ_h, 1);
+        const int ce = ctas_per_sm ? std::min(ctas_per_sm, std::max(occ_e, 1)) : std::max(occ_e, 1);
+        p->grid_h = p->nsm * ch;
+        p->grid_e = p->nsm * ce;
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->ps, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = cudaEventCreateWithFlags(&p->ev[b], cudaEventDisableTiming | cudaEventBlockingSync);
+        if (e == cudaSuccess) e = cudaMalloc(&p->d_tab[b], sizeof(PoolTable<float>));
+        if (e == cudaSuccess) e = cudaMemset(p->d_tab[b], 0, sizeof(PoolTable<float>));
+        if (e == cudaSuccess) e = cudaMallocHost(&p->h_tab[b], sizeof(PoolTable<float>));
+    }
+    // one graph per table: chunk_steps x (taps + counters, H pass, E pass)
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = cudaStreamSynchronize(p->ps);
+        cudaGraph_t gr = nullptr;
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(p->ps, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int s = 0; s < p->chunk; ++s) {
+                k_prologue_pool<float><<<kPoolMaxInst, 256, 0, p->ps>>>(p->d_tab[b]);
+                k_hpass_pool<float><<<p->grid_h, kPoolTpb, 0, p->ps>>>(p->d_tab[b]);
+                k_epass_pool<float><<<p->grid_e, kPoolTpb, 0, p->ps>>>(p->d_tab[b]);
+            }
+            e = cudaStreamEndCapture(p->ps, &gr);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b], gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+    }
+    if (e != cudaSuccess) {
+        int rc = pool_fail(nullptr, FIT_ERR_CUDA, "pool setup failed: %s", cudaGetErrorString(e));
+        pool_free(p);
+        return rc;
+    }
+    p->th = std::thread(pool_main, p);
+    *out = p;
+    return FIT_OK;
+}
+
+int fit_pool_destroy(FitPool* p) {
+    if (!p) return FIT_OK;
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->stop = true;
+    }
+    p->cv_work.notify_all();
+    if (p->th.joinable()) p->th.join();
+    pool_free(p);
+    return FIT_OK;
+}
+
+int fit_pool_last_error(const FitPool* p, char* buf, int64_t len) {
+    if (!buf || len <= 0) return FIT_ERR_ARG;
+    std::string m;
+    if (p) {
+        std::lock_guard<std::mutex> lk(const_cast<FitPool*>(p)->mu);
+        m = p->err;
+    } else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        m = g_create_error;
+    }
+    snprintf(buf, (size_t)len, "%s", m.c_str());
+    return FIT_OK;
+}
+
+int fit_pool_reserve(FitPool* p, int64_t bytes) {
+    if (!p || bytes < 0) return FIT_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (bytes > p->budget) {
+        p->err = "reservation larger than the pool budget";
+        return FIT_ERR_ARG;
+    }
+    if (p->reserved + bytes > p->budget) return FIT_ERR_BUDGET;
+    p->reserved += bytes;
+    return FIT_OK;
+}
+
+int fit_pool_release(FitPool* p, int64_t bytes) {
+    if (!p || bytes < 0) return FIT_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (bytes > p->reserved) {
+        p->err = "release of more bytes than reserved";
+        return FIT_ERR_ARG;
+    }
+    p->reserved -= bytes;
+    return FIT_OK;
+}
+
+int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t tag) {
+    if (!p || !c) return FIT_ERR_ARG;
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is already in a pool");
+    if (c->device != p->device) return fail(c, FIT_ERR_ARG, "context and pool are on different devices");
+    if (c->dtype != FIT_F32) return fail(c, FIT_ERR_ARG, "the pool steps FP32 contexts");
+    if (c->plane.active || c->abc_axes) return fail(c, FIT_ERR_ARG, "plane sources and ABC updates are not pooled");
+    if (n0 < 0 || nsteps <= 0) return fail(c, FIT_ERR_ARG, "bad step range");
+    if (c->beam.active && (!c->beam.dtieps || c->vt_len < n0 + nsteps))
+        return fail(c, FIT_ERR_STATE, "beam v*t table shorter than the run (%lld < %lld)", c->vt_len,
+                    (long long)(n0 + nsteps));
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        if (p->status != FIT_OK) return fail(c, p->status, "the pool stopped: %s", p->err.c_str());
+        if (p->stop) return fail(c, FIT_ERR_STATE, "the pool is stopping");
+    }
+    rc = enter(c);  // orders the caller's stream before the context stream
+    if (rc) return rc;
+    static thread_local long long host_n0;
+    host_n0 = n0;
+    CK(cudaMemcpyAsync(c->d_step, &host_n0, sizeof(long long), cudaMemcpyHostToDevice, c->own));
+    PoolSlot* s = new PoolSlot();
+    cudaError_t e = cudaEventCreateWithFlags(&s->ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ready, c->own);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->own);  // host_n0 is read before it changes
+    if (e != cudaSuccess) {
+        if (s->ready) cudaEventDestroy(s->ready);
+        delete s;
+        return fail(c, FIT_ERR_CUDA, "pool submit: %s", cudaGetErrorString(e));
+    }
+    s->c = c;
+    s->tag = tag;
+    s->nsteps = nsteps;
+    PoolInst<float>& r = s->row;
+    r.g = c->g;
+    r.mt = metric<float>(c);
+    r.E = static_cast<float*>(c->E);
+    r.H = static_cast<float*>(c->H);
+    r.ch = static_cast<const float*>(c->ch);
+    r.ce = static_cast<const float*>(c->ce);
+    r.cl = static_cast<const float*>(c->cl);
+    r.J = static_cast<float*>(c->J);
+    r.beam = c->beam;
+    r.tap = c->tap;
+    r.d_step = c->d_step;
+    r.vt_table = c->d_vt_table;
+    r.vt_len = c->vt_len;
+    r.n_end = n0 + nsteps;
+    r.vec = pick_vec(c);
+    r.nvec = c->g.N / r.vec;
+    r.mode = c->use_cond ? 1 : 0;
+    r.use_cond = c->use_cond;
+    s->ntiles = (r.nvec + kPoolTpb - 1) / kPoolTpb;
+    c->in_pool = true;
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        s->t_submit = p->now();
+        p->incoming.push_back(s);
+    }
+    p->cv_work.notify_all();
+    return FIT_OK;
+}
+
+int fit_pool_poll(FitPool* p, FitPoolDone* out, int32_t max, int32_t wait_ms) {
+    if (!p || (!out && max > 0) || max < 0) return FIT_ERR_ARG;
+    std::unique_lock<std::mutex> lk(p->mu);
+    if (p->done.empty() && wait_ms > 0 && (!p->active.empty() || !p->incoming.empty()))
+        p->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [p] { return !p->done.empty(); });
+    int n = 0;
+    while (n < max && !p->done.empty()) {
+        out[n++] = p->done.front();
+        p->done.pop_front();
+    }
+    return n;
+}
+
+int fit_pool_stats(FitPool* p, FitPoolStats* out) {
+    if (!p || !out) return FIT_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    FitPoolStats s{};
+    s.chunks = p->chunks;
+    s.cell_updates = p->cell_updates;
+    s.budget_bytes = p->budget;
+    s.reserved_bytes = p->reserved;
+    s.active = (int32_t)p->active.size();
+    s.queued = (int32_t)p->incoming.size();
+    s.max_active = p->max_active;
+    s.grid_h = p->grid_h;
+    s.grid_e = p->grid_e;
+    s.chunk_steps = p->chunk;
+    s.busy_ms = p->busy_ms;
+    *out = s;
+    return FIT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,355 @@
+"""Served wake solves: continuous batching of cavity wakefield requests on one GPU.
+
+There is no counterpart in the reference: Wakis runs one ``SolverFIT3D.wakesolve``
+(wakis/routines.py:231-485) per process.  This module keeps that call's inputs and
+outputs per request -- a ``GridFIT3D`` + ``WakeSolver`` + ``SolverFIT3D`` and the
+resulting ``WakeSolver.WP / WPx / WPy / Z / Zx / Zy`` -- and runs many requests through
+one ``libwakis_fit`` pool (``FitPool``), which steps all admitted grids together.
+
+Flow of a request:
+
+1. it arrives and waits in a queue;
+2. it is admitted when its device footprint (``footprint_bytes``) fits in the pool's
+   memory budget, and its solver is built: host setup, then the coefficient build and
+   the first step on the GPU;
+3. the pool takes its remaining steps in batched chunks, next to every other admitted
+   request; requests join and leave between chunks;
+4. when the pool reports it done, the wake potential is combined and the impedance is
+   taken (FP64, on the device); its memory is freed and released from the budget.
+
+Time-to-impedance is measured from arrival to the impedance on the host.
+"""
+
+import collections
+import dataclasses
+import math
+import tempfile
+import time
+
+import numpy as np
+
+from . import _native as nat
+
+MM = 1e-3
+
+
+@dataclasses.dataclass
+class CavityRequest:
+    """One wakefield solve of a cube cavity with a beam pipe (the cavity of config 0
+    scaled): vacuum = {|x|,|y|,|z| <= side/2} U {x^2 + y^2 <= rp^2}, domain
+    x, y in [-0.6 side, 0.6 side], z in [-1.2 side, 1.2 side], n x n x 2n cells.
+    sigma == 0: PEC walls (background PEC, ABC at the z ends, CFL 1.0).  sigma > 0: lossy
+    walls [1, 1, sigma] (relaxation form), 10-cell PML at the z ends, CFL 0.5 (the
+    explicit loss term is unstable at CFL 1.0)."""
+    tag: int
+    side: float
+    rp: float
+    n: int
+    sigmaz: float
+    sigma: float
+    arrival: float = 0.0
+    wakelength: float = 1.0
+    q: float = 1e-9
+    fmax: float = 5e9
+
+    @property
+    def cells(self):
+        return self.n * self.n * 2 * self.n
+
+    @property
+    def lossy(self):
+        return self.sigma > 0
+
+
+def config3_requests(count=64, seed=3, rate_hz=None, wakelength=1.0):
+    """The serving sweep's instances, drawn from numpy.random.default_rng(seed): cube side
+    U(20, 60) mm, pipe radius U(3, 8) mm, cells per transverse dimension uniform in
+    48..160 (z twice that), sigma_z U(5, 15) mm, walls PEC or lossy with sigma U(1e3, 1e6)
+    S/m (equal odds).  Arrivals form a Poisson stream of rate rate_hz (all at t = 0 when
+    rate_hz is None)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    for i in range(count):
+        side = rng.uniform(20, 60) * MM
+        rp = rng.uniform(3, 8) * MM
+        n = int(rng.integers(48, 161))
+        sigmaz = rng.uniform(5, 15) * MM
+        lossy = bool(rng.integers(0, 2))
+        sigma = float(rng.uniform(1e3, 1e6)) if lossy else 0.0
+        if rate_hz:
+            t += float(rng.exponential(1.0 / rate_hz))
+        out.append(CavityRequest(tag=i, side=side, rp=rp, n=n, sigmaz=sigmaz, sigma=sigma, arrival=t,
+                                 wakelength=wakelength))
+    return out
+
+
+def footprint_bytes(req, dtype=np.float32):
+    """Device bytes a request holds while it is served: E, H, J (3 x 3N field words), the
+    FP64 material tensors ieps, imu, sigma (3 x 3N x 8), the library's coefficient arrays
+    (ch, ce and, with losses, cl: 3N field words each), the cell mask and a fixed
+    allowance for the 1-D metrics, tap tables and allocator rounding."""
+    N = req.cells
+    w = np.dtype(dtype).itemsize
+    ncoef = 3 if req.lossy else 2
+    return int(N * (9 * w + 72 + 3 * w * ncoef + 1) + 8 * 2 ** 20)
+
+
+def _axes(req):
+    h, hz = 0.6 * req.side, 1.2 * req.side
+    return (np.linspace(-h, h, req.n + 1), np.linspace(-h, h, req.n + 1), np.linspace(-hz, hz, 2 * req.n + 1))
+
+
+def _vacuum_mask(req, device):
+    import torch
+    x, y, z = _axes(req)
+    xc, yc, zc = (torch.as_tensor(a[:-1] + np.diff(a) / 2, device=device) for a in (x, y, z))
+    X, Y, Z = xc[:, None, None], yc[None, :, None], zc[None, None, :]
+    half = req.side / 2
+    cube = (X.abs() <= half) & (Y.abs() <= half) & (Z.abs() <= half)
+    return cube | (X ** 2 + Y ** 2 <= req.rp ** 2)
+
+
+def cfl_dt(req, dtype=np.float32):
+    """The time step SolverFIT3D takes for the request, rounded to dtype (the solver's own
+    formula, wakis/solverFIT3D.py:294-307).  An FP64 solve given the FP32 step is the
+    FP64 reference of an FP32 solve: both then sample the wake at the same times."""
+    from scipy.constants import c as c_light
+    x, y, z = _axes(req)
+    cfln = 0.5 if req.lossy else 1.0
+    dt = cfln / (c_light * np.sqrt(1 / np.min(np.diff(x)) ** 2 + 1 / np.min(np.diff(y)) ** 2
+                                   + 1 / np.min(np.diff(z)) ** 2))
+    return float(np.dtype(dtype).type(dt))
+
+
+def build(req, dtype=np.float32, device=0, results_folder=None, dt=None):
+    """GridFIT3D, WakeSolver and SolverFIT3D of a request (cell-centre masks)."""
+    import torch
+    from .gridFIT3D import GridFIT3D
+    from .solverFIT3D import SolverFIT3D
+    from .wakeSolver import WakeSolver
+    dev = torch.device("cuda", device)
+    x, y, z = _axes(req)
+    vac = _vacuum_mask(req, dev)
+    if req.lossy:
+        grid = GridFIT3D(x=x, y=y, z=z, stl_solids={"walls": ~vac}, stl_materials={"walls": [1.0, 1.0, req.sigma]},
+                         verbose=0)
+        bc, bg, cfln = ["pec", "pec", "pml"], [1.0, 1.0], 0.5
+    else:
+        grid = GridFIT3D(x=x, y=y, z=z, stl_solids={"cavity": vac}, stl_materials={"cavity": "vacuum"}, verbose=0)
+        bc, bg, cfln = ["pec", "pec", "abc"], "pec", 1.0
+    del vac
+    wake = WakeSolver(wakelength=req.wakelength, q=req.q, sigmaz=req.sigmaz, beta=1.0, xsource=0.0, ysource=0.0,
+                      xtest=0.0, ytest=0.0, fmax=req.fmax, save=False, verbose=0,
+                      results_folder=results_folder or tempfile.gettempdir())
+    solver = SolverFIT3D(grid, wake, cfln=cfln, dt=dt, bc_low=bc, bc_high=bc, use_stl=True, bg=bg, dtype=dtype,
+                         n_pml=10, verbose=0)
+    return grid, wake, solver
+
+
+class ServedSolve:
+    """A request's solver between admission and its impedance."""
+
+    def __init__(self, req, dtype=np.float32, device=0, results_folder=None):
+        self.req = req
+        self.grid, self.wake, self.solver = build(req, dtype, device, results_folder)
+        s = self.solver
+        self.beam, self.Nt = s._wake_prepare(self.wake, req.wakelength, "both")
+        self.vt = s._wake_device_setup(self.beam, self.Nt)
+        self.first = s._wake_first_step(self.beam)
+        if s.step_0:
+            s._set_ghosts_to_0()
+            s.step_0 = False
+        s._sync_coeffs()
+
+    def submit(self, pool):
+        pool.submit(self.solver._ctx, self.first, self.Nt - self.first, self.req.tag)
+
+    def finish(self):
+        s = self.solver
+        s._run_steps += self.Nt - self.first
+        s._wake_device_done(self.vt, self.Nt)
+        self.wake.solve(compute_plane="both")
+        w = self.wake
+        return dict(s=w.s, WP=w.WP, WPx=w.WPx, WPy=w.WPy, f=w.f, Z=w.Z, Zx=w.Zx, Zy=w.Zy)
+
+    def close(self):
+        self.solver._ctx.close()
+        self.solver = self.wake = self.grid = self.beam = None
+
+
+def solve_alone(req, dtype=np.float32, device=0, dt=None):
+    """The request through the plain public API (SolverFIT3D.wakesolve), one at a time."""
+    grid, wake, solver = build(req, dtype, device, dt=dt)
+    solver.wakesolve(wakelength=req.wakelength, compute_plane="both")
+    out = dict(s=wake.s, WP=wake.WP, WPx=wake.WPx, WPy=wake.WPy, f=wake.f, Z=wake.Z, Zx=wake.Zx, Zy=wake.Zy,
+               Nt=solver.Nt, cells=req.cells)
+    solver._ctx.close()
+    return out
+
+
+def _percentile(v, p):
+    return float(np.percentile(np.asarray(v, dtype=np.float64), p)) if len(v) else None
+
+
+def summarize(records, makespan_s):
+    tti = [r["tti_s"] for r in records]
+    cells = sum(r["cells"] * r["steps"] for r in records)
+    return {"solves": len(records), "makespan_s": makespan_s,
+            "solves_per_hour": len(records) / makespan_s * 3600 if makespan_s > 0 else None,
+            "tti_p50_s": _percentile(tti, 50), "tti_p99_s": _percentile(tti, 99), "tti_max_s": max(tti) if tti else None,
+            "mcell_updates_per_s": cells / makespan_s / 1e6 if makespan_s > 0 else None}
+
+
+class Admission:
+    """First-fit admission in arrival order with bounded bypass.
+
+    ``admit(queue, size, reserve)`` walks the waiting requests oldest first and admits
+    (removes from ``queue`` and yields with its size) every request for which
+    ``reserve(size(req))`` succeeds.  A request admitted while an older one keeps waiting
+    counts as a bypass of the oldest; after ``max_bypass`` of them only the oldest may be
+    admitted, so a large request waits for at most that many smaller ones."""
+
+    def __init__(self, max_bypass=8):
+        self.max_bypass = max_bypass
+        self.bypass = 0
+        self._head = None
+
+    def admit(self, queue, size, reserve):
+        i = 0
+        while i < len(queue):
+            if queue[0] is not self._head:
+                self._head = queue[0]
+                self.bypass = 0
+            if i > 0 and self.bypass >= self.max_bypass:
+                return
+            req = queue[i]
+            nbytes = size(req)
+            if not reserve(nbytes):
+                i += 1
+                continue
+            queue.pop(i)
+            if i > 0:
+                self.bypass += 1
+            yield req, nbytes
+
+
+class ServingLoop:
+    """Continuous batching of requests through one FitPool.
+
+    Admission is first-fit in arrival order: a request that fits the free budget is
+    admitted even when an earlier one does not, unless the oldest waiting request has
+    already been passed over ``max_bypass`` times, after which admission is strict FIFO
+    until it gets in (bounded waiting for large requests)."""
+
+    def __init__(self, budget_bytes, chunk_steps=64, ctas_per_sm=0, device=0, dtype=np.float32, max_bypass=8,
+                 keep_results=True):
+        self.pool = nat.Pool(budget_bytes, chunk_steps=chunk_steps, ctas_per_sm=ctas_per_sm, device=device)
+        self.device = device
+        self.dtype = dtype
+        self.admission = Admission(max_bypass)
+        self.keep_results = keep_results
+        self.results = {}
+
+    def close(self):
+        self.pool.close()
+
+    def run(self, requests, time_scale=1.0):
+        """Serves the requests (arrival times in seconds, scaled by time_scale) and returns
+        per-request records and a summary."""
+        import torch
+        tmp = tempfile.mkdtemp()
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        queue = []
+        running = {}
+        records = []
+        t0 = time.perf_counter()
+        while pending or queue or running:
+            now = time.perf_counter() - t0
+            while pending and pending[0].arrival * time_scale <= now:
+                queue.append(pending.popleft())
+            admitted = False
+            for req, nbytes in self.admission.admit(queue, lambda r: footprint_bytes(r, self.dtype),
+                                                    self.pool.reserve):
+                t_adm = time.perf_counter() - t0
+                job = ServedSolve(req, self.dtype, self.device, tmp)
+                job.submit(self.pool)
+                running[req.tag] = (job, nbytes, t_adm, time.perf_counter() - t0)
+                admitted = True
+            if running:
+                if queue and not admitted:
+                    wait = 50
+                elif pending:
+                    wait = max(0, min(50, int((pending[0].arrival * time_scale - (time.perf_counter() - t0)) * 1e3)))
+                else:
+                    wait = 50
+                for d in self.pool.poll(wait_ms=wait):
+                    job, nbytes, t_adm, t_sub = running.pop(d["tag"])
+                    if d["status"] != 0:
+                        raise nat.FitError(d["status"], f"pooled solve {d['tag']} failed")
+                    res = job.finish()
+                    t_done = time.perf_counter() - t0
+                    req = job.req
+                    rec = dict(tag=req.tag, cells=req.cells, steps=job.Nt, lossy=req.lossy,
+                               arrival_s=req.arrival * time_scale, admitted_s=t_adm, submitted_s=t_sub,
+                               done_s=t_done, tti_s=t_done - req.arrival * time_scale,
+                               pool_ms=d["t_done_ms"] - d["t_submit_ms"], footprint=nbytes)
+                    records.append(rec)
+                    if self.keep_results:
+                        self.results[req.tag] = res
+                    job.close()
+                    del job
+                    torch.cuda.synchronize(self.device)
+                    self.pool.release(nbytes)
+            elif pending and not queue:
+                time.sleep(max(0.0, pending[0].arrival * time_scale - (time.perf_counter() - t0)))
+            elif queue and not admitted:
+                raise RuntimeError("a waiting request can never be admitted (footprint above the budget)")
+        makespan = time.perf_counter() - t0
+        out = summarize(records, makespan)
+        out["pool"] = self.pool.stats()
+        return records, out
+
+
+def serve_one_at_a_time(requests, dtype=np.float64, device=0, time_scale=1.0, dt_of=None, keep=None):
+    """Baseline: the same requests through SolverFIT3D.wakesolve one at a time (a single
+    server queue in arrival order), for time-to-impedance and solves/hour.  dt_of(req)
+    gives each solve's time step (None: the solver's own); keep, a dict, receives each
+    request's results by tag."""
+    import torch
+    reqs = sorted(requests, key=lambda r: r.arrival)
+    records = []
+    t0 = time.perf_counter()
+    for req in reqs:
+        now = time.perf_counter() - t0
+        if req.arrival * time_scale > now:
+            time.sleep(req.arrival * time_scale - now)
+        t_start = time.perf_counter() - t0
+        out = solve_alone(req, dtype, device, dt=dt_of(req) if dt_of else None)
+        torch.cuda.synchronize(device)
+        if keep is not None:
+            keep[req.tag] = out
+        t_done = time.perf_counter() - t0
+        records.append(dict(tag=req.tag, cells=req.cells, steps=out["Nt"], lossy=req.lossy,
+                            arrival_s=req.arrival * time_scale, admitted_s=t_start, done_s=t_done,
+                            tti_s=t_done - req.arrival * time_scale))
+        del out
+        torch.cuda.empty_cache()
+    return records, summarize(records, time.perf_counter() - t0)
+
+
+def poisson_rate_for(requests, budget_bytes, service_rate_cells_per_s, dtype=np.float32, load=1.5):
+    """An arrival rate at which admission by memory binds: requests arrive `load` times
+    faster than the GPU clears them, so the queue grows and the budget decides how many
+    run at once."""
+    work = np.mean([r.cells * _steps_estimate(r) for r in requests])
+    return load * service_rate_cells_per_s / work
+
+
+def _steps_estimate(req):
+    from scipy.constants import c as c_light
+    d = 1.2 * req.side / req.n
+    cfl = 0.5 if req.lossy else 1.0
+    dt = cfl / (c_light * math.sqrt(3.0 / d ** 2))
+    ti = 8.548921333333334 * req.sigmaz / c_light
+    return (req.wakelength + ti * c_light + 2.4 * req.side) / c_light / dt
