@@ -409,6 +409,136 @@ def run_accuracy(args):
     print(json.dumps({"accuracy": out}), flush=True)
 
 
+def run_serve(args):
+    """Served wake solves (the 64-request cavity sweep): FP32 continuous batching through
+    the pool against the plain FP64 path one request at a time, on the same requests and
+    Poisson arrivals; per-request WP / Z errors of the served FP32 results against the
+    FP64 ones (run at the FP32 time step); the pool's throughput with every request
+    resident; and the CPU oracle's per-core rate extrapolated to the same requests."""
+    import gc
+    import torch
+    import wakis_gb300 as wg  # noqa: F401  (builds / loads the library)
+    from wakis_gb300 import serving as S
+    from wakis_gb300 import _native as nat
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    peak, src = peaks()
+    budget = int(args.serve_budget_gb * 1e9)
+    base = S.config3_requests(args.serve_count, seed=3)
+    rate = S.poisson_rate_for(base, budget, args.serve_ref_rate * 1e9, load=args.serve_load)
+    reqs = S.config3_requests(args.serve_count, seed=3, rate_hz=rate)
+    work_bytes = {r.tag: (84 if r.lossy else 72) for r in reqs}
+
+    def model_bytes(recs):
+        return sum(work_bytes[r["tag"]] * r["cells"] * r["steps"] for r in recs)
+
+    # warm-up: library, graphs and allocator on two tiny requests
+    warm = [S.CavityRequest(tag=1000 + i, side=20e-3, rp=4e-3, n=16 + 2 * i, sigmaz=6e-3, sigma=1e4 * i,
+                            wakelength=0.05) for i in range(2)]
+    loop = S.ServingLoop(budget, chunk_steps=args.serve_chunk, keep_results=False)
+    loop.run(warm)
+    loop.close()
+
+    out = {"metric": METRIC, "impl": "ours", "mode": "serve", "n_gpus": 1, "dtype": "f32 fields, f64 wake sums and DFT",
+           "data": "synthetic (seeded cavity requests, analytic geometry)",
+           "config": {"workload": f"{len(reqs)} cavity wake solves (cube 20-60 mm, pipe 3-8 mm, n 48-160 cells, "
+                                  f"z 2n, sigma_z 5-15 mm, PEC or sigma 1e3-1e6 S/m, wake 1 m), "
+                                  f"default_rng(seed=3)",
+                      "budget_bytes": budget, "arrival_rate_hz": rate,
+                      "arrivals": f"Poisson, {args.serve_load}x the service rate of {args.serve_ref_rate} G "
+                                  f"cell-updates/s (the memory budget binds)",
+                      "chunk_steps": args.serve_chunk,
+                      "total_cell_updates": int(sum(r.cells * S._steps_estimate(r) for r in reqs))}}
+
+    # autotuner: pass-kernel variant per vector-width class, timed on calibration grids
+    t_tune = time.perf_counter()
+    tpool = nat.Pool(32 << 30, chunk_steps=args.serve_chunk)
+    tuned = S.autotune(tpool)
+    tpool.close()
+    gc.collect()
+    torch.cuda.empty_cache()
+    variants = {vec: r["choice"] for vec, r in tuned.items()}
+    out["autotune"] = {"seconds": time.perf_counter() - t_tune,
+                       "classes": {str(v): {"choice": r["choice"],
+                                            "G_cell_updates_per_s": {str(m): x / 1e9 for m, x in r["rates"].items()}}
+                                   for v, r in tuned.items()}}
+
+    # FP32 served
+    loop = S.ServingLoop(budget, chunk_steps=args.serve_chunk, variants=variants)
+    recs, summ = loop.run(reqs)
+    res32 = loop.results
+    loop.close()
+    gc.collect()
+    torch.cuda.empty_cache()
+    mb = model_bytes(recs)
+    summ["hbm_gbs_model"] = mb / summ["makespan_s"] / 1e9
+    summ["hbm_frac_model"] = summ["hbm_gbs_model"] / peak
+    busy = summ["pool"]["busy_ms"] / 1e3
+    summ["hbm_gbs_model_while_busy"] = mb / busy / 1e9 if busy > 0 else None
+    out["served_fp32"] = summ
+    out["value"] = summ["solves_per_hour"]
+    out["unit"] = "solves/h"
+    out["higher_is_better"] = True
+    out["tti_p50_s"], out["tti_p99_s"] = summ["tti_p50_s"], summ["tti_p99_s"]
+
+    # the pool with every request resident (kernel throughput of the batched passes)
+    if not args.serve_no_saturated:
+        jobs = [S.ServedSolve(r) for r in reqs]
+        pool = nat.Pool(sum(S.footprint_bytes(r) for r in reqs) + (1 << 30), chunk_steps=args.serve_chunk)
+        for vec, m in variants.items():
+            pool.tune(vec, m)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for j in jobs:
+            j.submit(pool)
+        done = []
+        while len(done) < len(jobs):
+            done += pool.poll(wait_ms=100)
+        el = time.perf_counter() - t0
+        st = pool.stats()
+        pool.close()
+        cu = sum(j.req.cells * (j.Nt - j.first) for j in jobs)
+        mbs = sum(work_bytes[j.req.tag] * j.req.cells * (j.Nt - j.first) for j in jobs)
+        two_pass = sum((108 if j.req.lossy else 96) * j.req.cells * (j.Nt - j.first) for j in jobs)
+        out["pool_all_resident"] = {"requests": len(jobs), "seconds": el, "mcell_updates_per_s": cu / el / 1e6,
+                                    "hbm_gbs_model": mbs / el / 1e9, "hbm_frac_model": mbs / el / 1e9 / peak,
+                                    "hbm_gbs_two_pass": two_pass / el / 1e9,
+                                    "hbm_frac_two_pass": two_pass / el / 1e9 / peak,
+                                    "chunks": st["chunks"], "variant": st["variant"], "grid": st["grid"],
+                                    "note": "72 B (PEC) / 84 B (lossy) per cell-update model; the two-pass "
+                                            "kernels move 96 / 108 B"}
+        for j in jobs:
+            j.close()
+        del jobs
+        gc.collect()
+        torch.cuda.empty_cache()
+
+    # FP64 one at a time, same arrivals, FP32 time step (accuracy reference)
+    if not args.serve_no_fp64:
+        res64 = {}
+        recs64, summ64 = S.serve_one_at_a_time(reqs, np.float64, dt_of=lambda r: S.cfl_dt(r, np.float32),
+                                               keep=res64)
+        out["plain_fp64_one_at_a_time"] = summ64
+        out["speedup_solves_per_hour"] = summ["solves_per_hour"] / summ64["solves_per_hour"]
+        out["speedup_tti_p99"] = summ64["tti_p99_s"] / summ["tti_p99_s"]
+        wp = [_rel(res32[t]["WP"], res64[t]["WP"]) for t in res32]
+        zz = [_rel(res32[t]["Z"], res64[t]["Z"]) for t in res32]
+        out["accuracy_vs_fp64"] = {"WP_rel_l2_max": max(wp), "WP_rel_l2_median": float(np.median(wp)),
+                                   "Z_rel_l2_max": max(zz), "Z_rel_l2_median": float(np.median(zz)),
+                                   "requests_above_1e-4": int(sum(e > 1e-4 for e in wp))}
+    if not args.no_cpu:
+        rate_cpu, sample, cores_used = cpu_sample_rate()
+        ncpu = os.cpu_count() or 1
+        mean_work = float(np.mean([r.cells * S._steps_estimate(r) for r in reqs]))
+        sec = mean_work / (rate_cpu * 1e6)
+        out["cpu_baseline"] = {"value": ncpu * 3600.0 / sec, "unit": "solves/h", "cores": ncpu, "kind": "port",
+                               "sample": f"{sample}: {rate_cpu:.2f} M cell-updates/s per core, extrapolated to "
+                                         f"the requests' mean {mean_work:.3e} cell-updates ({sec:.0f} s per solve), "
+                                         f"{ncpu} single-thread solves at once"}
+    print(json.dumps(out), flush=True)
+
+
 def profile_traffic():
     """DRAM bytes per E-pass launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "epass_cfg4_ncu.md")
@@ -434,6 +564,14 @@ def main():
     ap.add_argument("--grid", type=int, nargs=3, default=None)
     ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 errors on configs 1, 2 (and 4)")
     ap.add_argument("--accuracy-cfg4", action="store_true")
+    ap.add_argument("--serve", action="store_true", help="served wake solves: FP32 pool vs FP64 one at a time")
+    ap.add_argument("--serve-count", type=int, default=64)
+    ap.add_argument("--serve-budget-gb", type=float, default=4.0)
+    ap.add_argument("--serve-load", type=float, default=1.5)
+    ap.add_argument("--serve-ref-rate", type=float, default=60.0, help="G cell-updates/s setting the arrival rate")
+    ap.add_argument("--serve-chunk", type=int, default=64)
+    ap.add_argument("--serve-no-fp64", action="store_true")
+    ap.add_argument("--serve-no-saturated", action="store_true")
     ap.add_argument("--variant", default="direct", choices=["staged", "direct"],
                     help="pass kernels: direct-load kernels (default) or the persistent bulk-copy staged kernels")
     args = ap.parse_args()
@@ -442,7 +580,9 @@ def main():
     if world > 1 and args.impl == "ours":
         import torch
         torch.distributed.init_process_group("nccl")
-    if args.accuracy or args.accuracy_cfg4:
+    if args.serve:
+        run_serve(args)
+    elif args.accuracy or args.accuracy_cfg4:
         run_accuracy(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)

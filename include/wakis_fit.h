@@ -242,8 +242,9 @@ typedef struct FitPoolStats {
     int32_t active;         /* contexts in the work table or in flight */
     int32_t queued;         /* submitted, waiting for a table row */
     int32_t max_active;     /* most contexts stepped by one chunk */
-    int32_t grid_h, grid_e; /* persistent CTAs of the pooled H and E passes */
     int32_t chunk_steps;
+    int32_t variant[3];     /* pass-kernel variant (CTAs per SM) for vector widths 4, 2, 1 */
+    int32_t grid[3];        /* persistent CTAs of the E pass for vector widths 4, 2, 1 */
     double busy_ms;         /* host time with at least one chunk in flight */
 } FitPoolStats;
 
@@ -271,6 +272,12 @@ FIT_API int fit_pool_submit(FitPool *pool, FitCtx *ctx, int64_t n0, int64_t nste
  * wait_ms for the first one when none is ready and work is pending. */
 FIT_API int fit_pool_poll(FitPool *pool, FitPoolDone *out, int32_t max, int32_t wait_ms);
 FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
+/* Chooses the pass kernels of one vector-width class (vec = 4, 2 or 1 cells per vector,
+ * the widest that divides Nx): ctas_per_sm names the compiled variant by the CTAs per SM
+ * its register budget is sized for (vec 4: 2 or 3, vec 2: 2 or 3, vec 1: 3 or 4; the
+ * defaults are 3, 3 and 4).  Applies from the next chunk; graphs of the old variant are recaptured.
+ * The serving layer's autotuner times the variants on the requests' own grids. */
+FIT_API int fit_pool_tune(FitPool *pool, int32_t vec, int32_t ctas_per_sm);
 
 /* Library build information: sm architecture compiled for, and the kernel launch
  * counter (kernels issued since load), for bench accounting. */

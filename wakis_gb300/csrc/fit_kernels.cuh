@@ -1211,19 +1211,24 @@ __global__ void k_dft_reduce(const double2* __restrict__ part, int nsig, int nb,
 }
 
 // ---------------------------------------------------------------- batched (pool) kernels
-// Independent grids ("instances") advance together: one launch of each pass covers the
-// cells of every instance in a device work table.  The instances' flat index spaces are
-// laid end to end in tiles of kPoolTpb threads x vec cells; tile t belongs to the last
-// instance whose first tile is <= t, so a CTA works on one instance at a time and reads
-// that instance's descriptor from shared memory.  A persistent grid walks the tiles: its
-// size does not depend on the table, so one captured graph serves every mix, and the
-// table can change between graph replays.  Each instance keeps its own device step
+// Independent grids ("instances") advance together: one launch of a pass covers the
+// cells of every instance of one vector-width class in a device work table.  Rows are
+// ordered by class (4, 2, then 1 cells per vector: the widest that divides Nx) and each
+// instance's flat index space is cut into tiles of kPoolTpb vectors, laid end to end;
+// cls_t0 gives each class's tile range.  A persistent grid walks its class's tiles in
+// grid-stride order; a CTA reads the descriptor of the instance it is in into shared
+// memory and fetches the next one only when its tiles cross into another instance, so
+// most tiles run without a barrier.  The grid does not depend
+// on the table, so a captured graph serves every mix with the same classes present, and
+// the table can change between graph replays.  Each instance keeps its own device step
 // counter; an instance whose counter has reached its end is skipped, so instances that
-// finish inside a chunk of steps cost one descriptor fetch per tile from then on.  The
+// finish inside a chunk of steps cost one descriptor fetch per CTA from then on.  The
 // per-cell arithmetic is hpass_at / epass_at, the code of the single-grid kernels, so a
 // pooled instance gives bit-identical fields to the same grid run alone.
 constexpr int kPoolMaxInst = 64;
 constexpr int kPoolTpb = 256;
+
+__host__ __device__ constexpr int pool_class(int vec) { return vec == 4 ? 0 : (vec == 2 ? 1 : 2); }
 
 template <typename T>
 struct PoolInst {
@@ -1242,8 +1247,9 @@ struct PoolInst {
     long long vt_len;
     long long n_end;  // steps n < n_end are taken
     long long tile0;  // first tile of the instance
+    long long ntile;  // tiles of the instance: ceil(nvec / kPoolTpb)
     long long nvec;   // N / vec
-    int vec;          // cells per thread: 4, 2 or 1 (Nx % vec == 0)
+    int vec;          // cells per vector: 4, 2 or 1 (Nx % vec == 0)
     int mode;         // 0: lossless, 1: J = sigma*E folded into the loss factor
     int use_cond;
     int pad;
@@ -1253,7 +1259,7 @@ template <typename T>
 struct PoolTable {
     int ninst;
     int pad;
-    long long ntiles;
+    long long cls_t0[4];  // tiles of class c: [cls_t0[c], cls_t0[c+1])
     PoolInst<T> inst[kPoolMaxInst];
 };
 
@@ -1276,65 +1282,63 @@ __device__ __forceinline__ void pool_fetch(const PoolTable<T>* __restrict__ tab,
     if (threadIdx.x == 0) *step = *tab->inst[lo].d_step - 1;  // the prologue already advanced it
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kPoolTpb, 2) k_hpass_pool(const PoolTable<T>* __restrict__ tab) {
-    __shared__ PoolInst<T> si;
-    __shared__ long long sn;
+// Walks the class's tiles in grid-stride order, so the CTAs in flight sweep the flat
+// index space together and the +-row / +-plane neighbours of a tile are still in L2
+// from the tiles before it (as in the single-grid kernels); body(si, v) runs vector v
+// (instance-relative) of the instance in si, for the instances whose run has not ended.
+// The descriptor is fetched again only when the tile leaves the cached instance: the
+// test is uniform over the CTA, so the barriers around the fetch are too.
+template <typename T, int VEC, typename Body>
+__device__ __forceinline__ void pool_walk(const PoolTable<T>* __restrict__ tab, PoolInst<T>& si, long long& sn,
+                                          Body body) {
     const int ninst = tab->ninst;
-    const long long ntiles = tab->ntiles;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        pool_fetch<T>(tab, ninst, t, &si, &sn);
-        __syncthreads();
-        const long long v = (t - si.tile0) * kPoolTpb + threadIdx.x;
-        if (sn < si.n_end && v < si.nvec) {
-            if (si.vec == 4) {
-                if constexpr (sizeof(T) == 4) hpass_at<T, 4>(si.E, si.H, si.ch, si.g, si.mt, v * 4);
-            } else if (si.vec == 2) {
-                hpass_at<T, 2>(si.E, si.H, si.ch, si.g, si.mt, v * 2);
-            } else {
-                hpass_at<T, 1>(si.E, si.H, si.ch, si.g, si.mt, v);
-            }
+    const long long c0 = tab->cls_t0[pool_class(VEC)], c1 = tab->cls_t0[pool_class(VEC) + 1];
+    long long lo_t = 0, hi_t = -1;  // tile range of the cached descriptor
+    bool run = false;
+    for (long long t = c0 + blockIdx.x; t < c1; t += gridDim.x) {
+        if (t >= hi_t) {
+            __syncthreads();  // the previous descriptor is no longer read
+            pool_fetch<T>(tab, ninst, t, &si, &sn);
+            __syncthreads();
+            lo_t = si.tile0;
+            hi_t = si.tile0 + si.ntile;
+            run = sn < si.n_end;
         }
-        __syncthreads();
+        if (run) {
+            const long long v = (t - lo_t) * kPoolTpb + threadIdx.x;
+            if (v < si.nvec) body(si, v);
+        }
     }
 }
 
-template <typename T, int VEC>
-__device__ __forceinline__ void epass_pool_cells(const PoolInst<T>& si, long long n) {
-    StepArgs st{};
-    st.d_step = si.d_step;
-    st.vt_table = si.vt_table;
-    st.vt_len = si.vt_len;
-    const PlaneArgs pl{};
-    if (si.mode == 1)
-        epass_at<T, VEC, 1>(si.E, si.H, si.ce, si.cl, si.J, nullptr, nullptr, si.use_cond, si.g, si.mt, si.beam, pl,
-                            st, n);
-    else
-        epass_at<T, VEC, 0>(si.E, si.H, si.ce, si.cl, si.J, nullptr, nullptr, si.use_cond, si.g, si.mt, si.beam, pl,
-                            st, n);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kPoolTpb, 2) k_epass_pool(const PoolTable<T>* __restrict__ tab) {
+// MINB: CTAs per SM the register budget is sized for (the launch bound); the pool picks
+// one of the compiled variants per vector class.
+template <typename T, int VEC, int MINB>
+__global__ void __launch_bounds__(kPoolTpb, MINB) k_hpass_pool(const PoolTable<T>* __restrict__ tab) {
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
-    const int ninst = tab->ninst;
-    const long long ntiles = tab->ntiles;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        pool_fetch<T>(tab, ninst, t, &si, &sn);
-        __syncthreads();
-        const long long v = (t - si.tile0) * kPoolTpb + threadIdx.x;
-        if (sn < si.n_end && v < si.nvec) {
-            if (si.vec == 4) {
-                if constexpr (sizeof(T) == 4) epass_pool_cells<T, 4>(si, v * 4);
-            } else if (si.vec == 2) {
-                epass_pool_cells<T, 2>(si, v * 2);
-            } else {
-                epass_pool_cells<T, 1>(si, v);
-            }
-        }
-        __syncthreads();
-    }
+    pool_walk<T, VEC>(tab, si, sn, [](const PoolInst<T>& d, long long v) {
+        hpass_at<T, VEC>(d.E, d.H, d.ch, d.g, d.mt, v * VEC);
+    });
+}
+
+template <typename T, int VEC, int MINB>
+__global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T>* __restrict__ tab) {
+    __shared__ PoolInst<T> si;
+    __shared__ long long sn;
+    pool_walk<T, VEC>(tab, si, sn, [](const PoolInst<T>& d, long long v) {
+        StepArgs st{};
+        st.d_step = d.d_step;
+        st.vt_table = d.vt_table;
+        st.vt_len = d.vt_len;
+        const PlaneArgs pl{};
+        if (d.mode == 1)
+            epass_at<T, VEC, 1>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl, st,
+                                v * VEC);
+        else
+            epass_at<T, VEC, 0>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl, st,
+                                v * VEC);
+    });
 }
 
 // one block per table row: wake taps of E^n and the step counter (advanced past the

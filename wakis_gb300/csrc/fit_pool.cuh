@@ -5,12 +5,14 @@
 // driver thread per pool launches chunks and retires solves.  Shared state is guarded by
 // FitPool::mu.  The driver is the only thread that issues work on the pool stream.
 //
-// Chunks: chunk k replays graph k&1, which reads device table k&1 (rows = member
-// contexts).  Up to two chunks are in flight; before the table of chunk k+1 is staged
-// into pinned buffer (k+1)&1 the driver has waited for chunk k-1, the last user of that
-// buffer and of its device table.  Which contexts a chunk finishes is known on the host
-// when it is launched (every member takes min(chunk, remaining) steps), so no device
-// state is read back between chunks.
+// Chunks: chunk k reads device table k&1 (rows = member contexts, ordered by vector
+// width class) and replays the graph of that table and of the classes present (captured
+// on first use: chunk_steps x [taps + counters, the H pass of each class present, the
+// E pass of each class present]).  Up to two chunks are in flight; before the table of
+// chunk k+1 is staged into pinned buffer (k+1)&1 the driver has waited for chunk k-1,
+// the last user of that buffer and of its device table.  Which contexts a chunk
+// finishes is known on the host when it is launched (every member takes min(chunk,
+// remaining) steps), so no device state is read back between chunks.
 #include <chrono>
 #include <condition_variable>
 #include <cstddef>
@@ -43,12 +45,17 @@ struct FitPool {
     int device = 0;
     int nsm = 1;
     int chunk = 64;
-    int grid_h = 0, grid_e = 0;
-    cudaStream_t ps = nullptr;
+    int ctas_per_sm = 0;
+    int minb[3]{3, 3, 4};          // kernel variant (CTAs per SM of its register budget) per class
+    int grid_h[3]{}, grid_e[3]{};  // persistent CTAs of the pass kernels per vector class
+    int gen = 0;                   // bumped by fit_pool_tune: captured graphs of older variants are stale
+    cudaStream_t ps = nullptr;     // every chunk runs here
+    cudaStream_t cs = nullptr;     // idle stream the graphs are captured on
     cudaEvent_t ev[2]{};
     PoolTable<float>* d_tab[2]{};
     PoolTable<float>* h_tab[2]{};
-    cudaGraphExec_t graph[2]{};
+    cudaGraphExec_t graph[2][8]{};  // [table][mask of the classes present]
+    int graph_gen[2][8]{};
     long long budget = 0, reserved = 0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -117,21 +124,110 @@ void pool_abort(FitPool* p, cudaError_t e, const char* what) {
     p->cv_done.notify_all();
 }
 
-// fills pinned table `b` with the members that still have steps to enqueue
-int stage_table(FitPool* p, int b, std::vector<PoolSlot*>& members) {
+// fills pinned table `b` with the members that still have steps to enqueue, ordered by
+// vector class; returns the mask of the classes present
+int stage_table(FitPool* p, int b, const std::vector<PoolSlot*>& members) {
     PoolTable<float>* t = p->h_tab[b];
     long long tile = 0;
-    int n = 0;
-    for (PoolSlot* s : members) {
-        PoolInst<float>& r = t->inst[n++];
-        r = s->row;
-        r.tile0 = tile;
-        tile += s->ntiles;
+    int n = 0, mask = 0;
+    for (int cls = 0; cls < 3; ++cls) {
+        t->cls_t0[cls] = tile;
+        for (PoolSlot* s : members) {
+            if (pool_class(s->row.vec) != cls) continue;
+            PoolInst<float>& r = t->inst[n++];
+            r = s->row;
+            r.tile0 = tile;
+            tile += s->ntiles;
+            mask |= 1 << cls;
+        }
     }
+    t->cls_t0[3] = tile;
     t->ninst = n;
-    t->ntiles = tile;
-    return n;
+    return mask;
 }
+
+// compiled variants: launch bound (CTAs per SM) choices per vector class
+constexpr int kPoolMinb[3][2] = {{2, 3}, {2, 3}, {3, 4}};
+
+bool pool_minb_ok(int cls, int minb) { return minb == kPoolMinb[cls][0] || minb == kPoolMinb[cls][1]; }
+
+template <int VEC, int MINB>
+cudaError_t pool_occupancy(int* h, int* e) {
+    cudaError_t r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(h, k_hpass_pool<float, VEC, MINB>, kPoolTpb, 0);
+    if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(e, k_epass_pool<float, VEC, MINB>, kPoolTpb, 0);
+    return r;
+}
+
+// persistent grids of class cls with variant minb (capped by ctas_per_sm when set)
+cudaError_t pool_grids(int nsm, int cls, int minb, int ctas_per_sm, int* gh, int* ge) {
+    int oh = 0, oe = 0;
+    cudaError_t e;
+    if (cls == 0)
+        e = minb == 2 ? pool_occupancy<4, 2>(&oh, &oe) : pool_occupancy<4, 3>(&oh, &oe);
+    else if (cls == 1)
+        e = minb == 2 ? pool_occupancy<2, 2>(&oh, &oe) : pool_occupancy<2, 3>(&oh, &oe);
+    else
+        e = minb == 3 ? pool_occupancy<1, 3>(&oh, &oe) : pool_occupancy<1, 4>(&oh, &oe);
+    oh = std::max(oh, 1);
+    oe = std::max(oe, 1);
+    *gh = nsm * (ctas_per_sm ? std::min(ctas_per_sm, oh) : oh);
+    *ge = nsm * (ctas_per_sm ? std::min(ctas_per_sm, oe) : oe);
+    return e;
+}
+
+struct PoolTune {
+    int minb[3], grid_h[3], grid_e[3], gen;
+};
+
+template <int VEC, int MINB>
+void launch_pool_pass(const PoolTune& t, PoolTable<float>* tab, cudaStream_t st, bool e_pass) {
+    const int c = pool_class(VEC);
+    if (e_pass)
+        k_epass_pool<float, VEC, MINB><<<t.grid_e[c], kPoolTpb, 0, st>>>(tab);
+    else
+        k_hpass_pool<float, VEC, MINB><<<t.grid_h[c], kPoolTpb, 0, st>>>(tab);
+}
+
+void launch_pool_class(const PoolTune& t, int cls, PoolTable<float>* tab, cudaStream_t st, bool e_pass) {
+    const int m = t.minb[cls];
+    if (cls == 0)
+        m == 2 ? launch_pool_pass<4, 2>(t, tab, st, e_pass) : launch_pool_pass<4, 3>(t, tab, st, e_pass);
+    else if (cls == 1)
+        m == 2 ? launch_pool_pass<2, 2>(t, tab, st, e_pass) : launch_pool_pass<2, 3>(t, tab, st, e_pass);
+    else
+        m == 3 ? launch_pool_pass<1, 3>(t, tab, st, e_pass) : launch_pool_pass<1, 4>(t, tab, st, e_pass);
+}
+
+// the graph of table b with the classes in mask, captured on the idle capture stream
+cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraphExec_t* out) {
+    if (p->graph[b][mask] && p->graph_gen[b][mask] == t.gen) {
+        *out = p->graph[b][mask];
+        return cudaSuccess;
+    }
+    if (p->graph[b][mask]) {
+        cudaGraphExecDestroy(p->graph[b][mask]);
+        p->graph[b][mask] = nullptr;
+    }
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    for (int s = 0; s < p->chunk; ++s) {
+        k_prologue_pool<float><<<kPoolMaxInst, 256, 0, p->cs>>>(p->d_tab[b]);
+        for (int pass = 0; pass < 2; ++pass)
+            for (int cls = 0; cls < 3; ++cls)
+                if (mask & (1 << cls)) launch_pool_class(t, cls, p->d_tab[b], p->cs, pass == 1);
+    }
+    e = cudaStreamEndCapture(p->cs, &gr);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b][mask], gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    if (e == cudaSuccess) {
+        p->graph_gen[b][mask] = t.gen;
+        *out = p->graph[b][mask];
+    }
+    return e;
+}
+
+int popcount3(int m) { return (m & 1) + ((m >> 1) & 1) + ((m >> 2) & 1); }
 
 void pool_main(FitPool* p) {
     if (cudaSetDevice(p->device) != cudaSuccess) {
@@ -144,6 +240,7 @@ void pool_main(FitPool* p) {
     for (;;) {
         std::vector<PoolSlot*> members;
         bool launch = false;
+        PoolTune tune{};
         {
             std::unique_lock<std::mutex> lk(p->mu);
             if (p->stop && fl.empty()) break;
@@ -159,12 +256,20 @@ void pool_main(FitPool* p) {
                 for (PoolSlot* s : p->active)
                     if (s->sched < s->nsteps) members.push_back(s);
                 launch = !members.empty() && fl.size() < 2;
+                for (int c = 0; c < 3; ++c) {
+                    tune.minb[c] = p->minb[c];
+                    tune.grid_h[c] = p->grid_h[c];
+                    tune.grid_e[c] = p->grid_e[c];
+                }
+                tune.gen = p->gen;
             }
         }
         if (launch) {
             const int b = (int)(k & 1);
-            const int n = stage_table(p, b, members);
-            cudaError_t e = cudaSuccess;
+            const int mask = stage_table(p, b, members);
+            const int n = (int)members.size();
+            cudaGraphExec_t gx = nullptr;
+            cudaError_t e = pool_graph(p, tune, b, mask, &gx);
             for (PoolSlot* s : members)
                 if (!s->joined && e == cudaSuccess) {
                     e = cudaStreamWaitEvent(p->ps, s->ready, 0);
@@ -172,13 +277,13 @@ void pool_main(FitPool* p) {
                 }
             const size_t bytes = offsetof(PoolTable<float>, inst) + (size_t)n * sizeof(PoolInst<float>);
             if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_tab[b], p->h_tab[b], bytes, cudaMemcpyHostToDevice, p->ps);
-            if (e == cudaSuccess) e = cudaGraphLaunch(p->graph[b], p->ps);
+            if (e == cudaSuccess) e = cudaGraphLaunch(gx, p->ps);
             if (e == cudaSuccess) e = cudaEventRecord(p->ev[b], p->ps);
             if (e != cudaSuccess) {
                 pool_abort(p, e, "pool chunk launch");
                 break;
             }
-            g_launches += 3LL * p->chunk;
+            g_launches += (1LL + 2LL * popcount3(mask)) * p->chunk;
             InFlight f;
             f.buf = b;
             f.t_launch = p->now();
@@ -236,12 +341,14 @@ void pool_free(FitPool* p) {
     cudaSetDevice(p->device);
     if (p->ps) cudaStreamSynchronize(p->ps);
     for (int b = 0; b < 2; ++b) {
-        if (p->graph[b]) cudaGraphExecDestroy(p->graph[b]);
+        for (int m = 0; m < 8; ++m)
+            if (p->graph[b][m]) cudaGraphExecDestroy(p->graph[b][m]);
         if (p->ev[b]) cudaEventDestroy(p->ev[b]);
         if (p->d_tab[b]) cudaFree(p->d_tab[b]);
         if (p->h_tab[b]) cudaFreeHost(p->h_tab[b]);
     }
     if (p->ps) cudaStreamDestroy(p->ps);
+    if (p->cs) cudaStreamDestroy(p->cs);
     delete p;
 }
 
@@ -266,38 +373,18 @@ int fit_pool_create(int32_t device, int64_t budget_bytes, int32_t chunk_steps, i
     p->t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, device);
-    int occ_h = 0, occ_e = 0;
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_h, k_hpass_pool<float>, kPoolTpb, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_epass_pool<float>, kPoolTpb, 0);
-    if (e == cudaSuccess) {
-        const int ch = ctas_per_sm ? std::min(ctas_per_sm, std::max(occ_h, 1)) : std::max(occ_h, 1);
-        const int ce = ctas_per_sm ? std::min(ctas_per_sm, std::max(occ_e, 1)) : std::max(occ_e, 1);
-        p->grid_h = p->nsm * ch;
-        p->grid_e = p->nsm * ce;
-    }
+    p->ctas_per_sm = ctas_per_sm;
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+        e = pool_grids(p->nsm, c, p->minb[c], ctas_per_sm, &p->grid_h[c], &p->grid_e[c]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->ps, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cs, cudaStreamNonBlocking);
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         e = cudaEventCreateWithFlags(&p->ev[b], cudaEventDisableTiming | cudaEventBlockingSync);
         if (e == cudaSuccess) e = cudaMalloc(&p->d_tab[b], sizeof(PoolTable<float>));
         if (e == cudaSuccess) e = cudaMemset(p->d_tab[b], 0, sizeof(PoolTable<float>));
         if (e == cudaSuccess) e = cudaMallocHost(&p->h_tab[b], sizeof(PoolTable<float>));
     }
-    // one graph per table: chunk_steps x (taps + counters, H pass, E pass)
-    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
-        e = cudaStreamSynchronize(p->ps);
-        cudaGraph_t gr = nullptr;
-        if (e == cudaSuccess) e = cudaStreamBeginCapture(p->ps, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            for (int s = 0; s < p->chunk; ++s) {
-                k_prologue_pool<float><<<kPoolMaxInst, 256, 0, p->ps>>>(p->d_tab[b]);
-                k_hpass_pool<float><<<p->grid_h, kPoolTpb, 0, p->ps>>>(p->d_tab[b]);
-                k_epass_pool<float><<<p->grid_e, kPoolTpb, 0, p->ps>>>(p->d_tab[b]);
-            }
-            e = cudaStreamEndCapture(p->ps, &gr);
-        }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b], gr, 0);
-        if (gr) cudaGraphDestroy(gr);
-    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->ps);
     if (e != cudaSuccess) {
         int rc = pool_fail(nullptr, FIT_ERR_CUDA, "pool setup failed: %s", cudaGetErrorString(e));
         pool_free(p);
@@ -410,7 +497,8 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     r.nvec = c->g.N / r.vec;
     r.mode = c->use_cond ? 1 : 0;
     r.use_cond = c->use_cond;
-    s->ntiles = (r.nvec + kPoolTpb - 1) / kPoolTpb;
+    r.ntile = (r.nvec + kPoolTpb - 1) / kPoolTpb;
+    s->ntiles = r.ntile;
     c->in_pool = true;
     {
         std::lock_guard<std::mutex> lk(p->mu);
@@ -434,6 +522,26 @@ int fit_pool_poll(FitPool* p, FitPoolDone* out, int32_t max, int32_t wait_ms) {
     return n;
 }
 
+int fit_pool_tune(FitPool* p, int32_t vec, int32_t ctas_per_sm) {
+    if (!p || (vec != 4 && vec != 2 && vec != 1)) return FIT_ERR_ARG;
+    const int cls = pool_class(vec);
+    if (!pool_minb_ok(cls, ctas_per_sm)) {
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->err = "no compiled pool kernel variant for that vector width and CTAs per SM";
+        return FIT_ERR_ARG;
+    }
+    int gh = 0, ge = 0;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e == cudaSuccess) e = pool_grids(p->nsm, cls, ctas_per_sm, p->ctas_per_sm, &gh, &ge);
+    if (e != cudaSuccess) return pool_fail(p, FIT_ERR_CUDA, "fit_pool_tune: %s", cudaGetErrorString(e));
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->minb[cls] = ctas_per_sm;
+    p->grid_h[cls] = gh;
+    p->grid_e[cls] = ge;
+    p->gen++;
+    return FIT_OK;
+}
+
 int fit_pool_stats(FitPool* p, FitPoolStats* out) {
     if (!p || !out) return FIT_ERR_ARG;
     std::lock_guard<std::mutex> lk(p->mu);
@@ -445,8 +553,10 @@ int fit_pool_stats(FitPool* p, FitPoolStats* out) {
     s.active = (int32_t)p->active.size();
     s.queued = (int32_t)p->incoming.size();
     s.max_active = p->max_active;
-    s.grid_h = p->grid_h;
-    s.grid_e = p->grid_e;
+    for (int c = 0; c < 3; ++c) {
+        s.variant[c] = p->minb[c];
+        s.grid[c] = p->grid_e[c];
+    }
     s.chunk_steps = p->chunk;
     s.busy_ms = p->busy_ms;
     *out = s;

@@ -188,6 +188,70 @@ def solve_alone(req, dtype=np.float32, device=0, dt=None):
     return out
 
 
+POOL_VARIANTS = {4: (2, 3), 2: (2, 3), 1: (3, 4)}
+
+
+def run_resident(pool, reqs):
+    """Builds every request, submits them together and waits: returns (cell-updates,
+    seconds of pool time with chunks in flight, jobs)."""
+    jobs = [ServedSolve(r) for r in reqs]
+    busy0 = pool.stats()["busy_ms"]
+    for j in jobs:
+        j.submit(pool)
+    done = []
+    while len(done) < len(jobs):
+        done += pool.poll(wait_ms=50)
+    if any(d["status"] != 0 for d in done):
+        raise nat.FitError(min(d["status"] for d in done), "pooled calibration solve failed")
+    busy = (pool.stats()["busy_ms"] - busy0) / 1e3
+    return sum(j.req.cells * (j.Nt - j.first) for j in jobs), busy, jobs
+
+
+def calibration_requests(seed=11, per_class=4, wakelength=0.1):
+    """Grids of the serving sweep's distribution (config3_requests' ranges) with Nx forced
+    into each vector-width class: per class, per_class requests, half of them lossy."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    tag = 10000
+    for vec in (4, 2, 1):
+        reqs = []
+        for i in range(per_class):
+            n = int(rng.integers(48, 157))
+            n = n - n % 4 + {4: 0, 2: 2, 1: 1}[vec]
+            reqs.append(CavityRequest(tag=tag, side=rng.uniform(20, 60) * MM, rp=rng.uniform(3, 8) * MM, n=n,
+                                      sigmaz=rng.uniform(5, 15) * MM, sigma=(float(rng.uniform(1e3, 1e6)) if i % 2
+                                                                               else 0.0), wakelength=wakelength))
+            tag += 1
+        out[vec] = reqs
+    return out
+
+
+def autotune(pool, calib=None, repeats=1):
+    """Per vector-width class, times every compiled pass-kernel variant of the pool on
+    calibration grids (all resident at once, pool time only) and keeps the fastest.
+    Returns {vec: {"choice": ctas_per_sm, "rates": {variant: cell-updates/s}}}."""
+    import torch
+    calib = calib or calibration_requests()
+    out = {}
+    for vec, reqs in calib.items():
+        rates = {}
+        for minb in POOL_VARIANTS[vec]:
+            pool.tune(vec, minb)
+            best = 0.0
+            for _ in range(repeats):
+                cu, busy, jobs = run_resident(pool, reqs)
+                for j in jobs:
+                    j.close()
+                del jobs
+                torch.cuda.empty_cache()
+                best = max(best, cu / busy if busy > 0 else 0.0)
+            rates[minb] = best
+        choice = max(rates, key=rates.get)
+        pool.tune(vec, choice)
+        out[vec] = {"choice": choice, "rates": rates}
+    return out
+
+
 def _percentile(v, p):
     return float(np.percentile(np.asarray(v, dtype=np.float64), p)) if len(v) else None
 
@@ -243,8 +307,10 @@ class ServingLoop:
     until it gets in (bounded waiting for large requests)."""
 
     def __init__(self, budget_bytes, chunk_steps=64, ctas_per_sm=0, device=0, dtype=np.float32, max_bypass=8,
-                 keep_results=True):
+                 keep_results=True, variants=None):
         self.pool = nat.Pool(budget_bytes, chunk_steps=chunk_steps, ctas_per_sm=ctas_per_sm, device=device)
+        for vec, minb in (variants or {}).items():
+            self.pool.tune(vec, minb)
         self.device = device
         self.dtype = dtype
         self.admission = Admission(max_bypass)
