@@ -114,17 +114,35 @@ int fail(FitCtx* c, int code, const char* fmt, ...) {
 
 size_t esize(const FitCtx* c) { return c->dtype == FIT_F64 ? 8 : 4; }
 
+// Device buffers are stream-ordered allocations (cudaMallocAsync / cudaFreeAsync) on the
+// context stream: a plain cudaFree waits for the whole device, including the kernels of
+// other contexts and of a serving pool, while the stream-ordered calls wait for nothing.
+// The device's default memory pool keeps freed blocks for reuse (release threshold set
+// to the maximum once per device), like a caching allocator.
+void keep_freed_blocks(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    cudaMemPool_t mp;
+    if (cudaDeviceGetDefaultMemPool(&mp, device) == cudaSuccess) {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done.push_back(device);
+}
+
 int dev_alloc(FitCtx* c, void** p, size_t bytes) {
     if (*p) {
-        cudaFree(*p);
+        cudaFreeAsync(*p, c->own);
         *p = nullptr;
     }
     if (bytes == 0) return FIT_OK;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = cudaMallocAsync(p, bytes, c->own);
     if (e != cudaSuccess) {
         *p = nullptr;
         return fail(c, e == cudaErrorMemoryAllocation ? FIT_ERR_NOMEM : FIT_ERR_CUDA,
-                    "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+                    "cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
     }
     return FIT_OK;
 }
@@ -137,8 +155,8 @@ int upload(FitCtx* c, P** dst, const void* src, size_t bytes) {
     return FIT_OK;
 }
 
-void dfree(void* p) {
-    if (p) cudaFree(p);
+void dfree(void* p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
 }
 
 // ordering with the caller's stream
@@ -382,9 +400,10 @@ int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_step, sizeof(long long));
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) keep_freed_blocks(c->device);
+    if (e == cudaSuccess) e = cudaMallocAsync(&c->d_step, sizeof(long long), c->own);
+    if (e == cudaSuccess) e = cudaMallocAsync(&c->d_err, sizeof(int), c->own);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->own);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) {
         int rc = fail(nullptr, FIT_ERR_CUDA, "context setup failed: %s", cudaGetErrorString(e));
@@ -411,18 +430,19 @@ int fit_ctx_destroy(FitCtx* c) {
     if (c->own) cudaStreamSynchronize(c->own);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     for (int a = 0; a < 3; ++a) {
-        dfree(c->dL[a]);
-        dfree(c->dtL0[a]);
-        dfree(c->tL_T[a]);
-        dfree(c->L_T[a]);
+        dfree(c->dL[a], c->own);
+        dfree(c->dtL0[a], c->own);
+        dfree(c->tL_T[a], c->own);
+        dfree(c->L_T[a], c->own);
     }
-    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg}) dfree(p);
+    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg}) dfree(p, c->own);
     for (void* p : {(void*)c->d_beam_z, (void*)c->d_beam_dtieps, (void*)c->d_vt_table, (void*)c->d_prof,
                     (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
                     (void*)c->d_em, (void*)c->d_ek0, (void*)c->d_ecnt, (void*)c->d_dz, (void*)c->d_acc,
                     (void*)c->d_comp, (void*)c->d_scratch, (void*)c->d_wp3d, (void*)c->d_wpx, (void*)c->d_wpy,
                     (void*)c->d_step, (void*)c->d_err})
-        dfree(p);
+        dfree(p, c->own);
+    if (c->own) cudaStreamSynchronize(c->own);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
     if (c->own) cudaStreamDestroy(c->own);
@@ -632,7 +652,7 @@ int fit_set_plane_source(FitCtx* c, int32_t active, int32_t zs, int32_t x0, int3
     if (prof) {
         rc = upload(c, &c->d_prof, prof, np * sizeof(double));
     } else {
-        dfree(c->d_prof);
+        dfree(c->d_prof, c->own);
         c->d_prof = nullptr;
     }
     if (!rc) rc = upload(c, &c->d_c1, c1, n * sizeof(double));
@@ -872,7 +892,6 @@ int fit_wake_finalize(FitCtx* c, double qscale, double ds, double dxf, double dy
 }
 
 int fit_dft(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb, double* out) {
-    FitCtx* c = nullptr;
     if (!x || !out || nsig <= 0 || len <= 0 || n <= 0 || nb <= 0 || b0 < 0)
         return fail(nullptr, FIT_ERR_ARG, "bad fit_dft arguments");
     const int nsplit = (int)std::max<long long>(1, std::min<long long>(32, len / 2048));
@@ -881,16 +900,21 @@ int fit_dft(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, i
     double2* dout = nullptr;
     cudaStream_t s = nullptr;
     auto cleanup = [&]() {
-        if (s) cudaStreamSynchronize(s);
-        dfree(dx);
-        dfree(part);
-        dfree(dout);
-        if (s) cudaStreamDestroy(s);
+        if (s) {
+            dfree(dx, s);
+            dfree(part, s);
+            dfree(dout, s);
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
     };
-    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&dx, (size_t)nsig * len * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&part, (size_t)nsig * nsplit * nb * sizeof(double2));
-    if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)nsig * nb * sizeof(double2));
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) keep_freed_blocks(dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dx, (size_t)nsig * len * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&part, (size_t)nsig * nsplit * nb * sizeof(double2), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dout, (size_t)nsig * nb * sizeof(double2), s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)nsig * len * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) {
         cleanup();

@@ -6,7 +6,7 @@
 // FitPool::mu.  The driver is the only thread that issues work on the pool stream.
 //
 // Chunks: chunk k reads device table k&1 (rows = member contexts, ordered by vector
-// width class) and replays the graph of that table and of the classes present (captured
+// width class) and replays the graph of that table and of the classes present (built
 // on first use: chunk_steps x [taps + counters, the H pass of each class present, the
 // E pass of each class present]).  Up to two chunks are in flight; before the table of
 // chunk k+1 is staged into pinned buffer (k+1)&1 the driver has waited for chunk k-1,
@@ -50,7 +50,6 @@ struct FitPool {
     int grid_h[3]{}, grid_e[3]{};  // persistent CTAs of the pass kernels per vector class
     int gen = 0;                   // bumped by fit_pool_tune: captured graphs of older variants are stale
     cudaStream_t ps = nullptr;     // every chunk runs here
-    cudaStream_t cs = nullptr;     // idle stream the graphs are captured on
     cudaEvent_t ev[2]{};
     PoolTable<float>* d_tab[2]{};
     PoolTable<float>* h_tab[2]{};
@@ -179,26 +178,38 @@ struct PoolTune {
     int minb[3], grid_h[3], grid_e[3], gen;
 };
 
-template <int VEC, int MINB>
-void launch_pool_pass(const PoolTune& t, PoolTable<float>* tab, cudaStream_t st, bool e_pass) {
-    const int c = pool_class(VEC);
-    if (e_pass)
-        k_epass_pool<float, VEC, MINB><<<t.grid_e[c], kPoolTpb, 0, st>>>(tab);
-    else
-        k_hpass_pool<float, VEC, MINB><<<t.grid_h[c], kPoolTpb, 0, st>>>(tab);
-}
-
-void launch_pool_class(const PoolTune& t, int cls, PoolTable<float>* tab, cudaStream_t st, bool e_pass) {
-    const int m = t.minb[cls];
+// kernel entry of class cls's pass with variant m
+const void* pool_pass_func(int cls, int m, bool e_pass) {
     if (cls == 0)
-        m == 2 ? launch_pool_pass<4, 2>(t, tab, st, e_pass) : launch_pool_pass<4, 3>(t, tab, st, e_pass);
-    else if (cls == 1)
-        m == 2 ? launch_pool_pass<2, 2>(t, tab, st, e_pass) : launch_pool_pass<2, 3>(t, tab, st, e_pass);
-    else
-        m == 3 ? launch_pool_pass<1, 3>(t, tab, st, e_pass) : launch_pool_pass<1, 4>(t, tab, st, e_pass);
+        return e_pass ? (m == 2 ? (const void*)k_epass_pool<float, 4, 2> : (const void*)k_epass_pool<float, 4, 3>)
+                      : (m == 2 ? (const void*)k_hpass_pool<float, 4, 2> : (const void*)k_hpass_pool<float, 4, 3>);
+    if (cls == 1)
+        return e_pass ? (m == 2 ? (const void*)k_epass_pool<float, 2, 2> : (const void*)k_epass_pool<float, 2, 3>)
+                      : (m == 2 ? (const void*)k_hpass_pool<float, 2, 2> : (const void*)k_hpass_pool<float, 2, 3>);
+    return e_pass ? (m == 3 ? (const void*)k_epass_pool<float, 1, 3> : (const void*)k_epass_pool<float, 1, 4>)
+                  : (m == 3 ? (const void*)k_hpass_pool<float, 1, 3> : (const void*)k_hpass_pool<float, 1, 4>);
 }
 
-// the graph of table b with the classes in mask, captured on the idle capture stream
+// appends one kernel node after *prev (graphs are built node by node, not captured, so
+// building one never interferes with device-wide synchronisation by other threads)
+cudaError_t add_node(cudaGraph_t g, cudaGraphNode_t* prev, const void* func, int grid, int block,
+                     PoolTable<float>* tab) {
+    void* args[1] = {&tab};
+    cudaKernelNodeParams kp{};
+    kp.func = const_cast<void*>(func);
+    kp.gridDim = dim3((unsigned)grid);
+    kp.blockDim = dim3((unsigned)block);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    cudaGraphNode_t node = nullptr;
+    cudaError_t e = cudaGraphAddKernelNode(&node, g, *prev ? prev : nullptr, *prev ? 1 : 0, &kp);
+    if (e == cudaSuccess) *prev = node;
+    return e;
+}
+
+// the graph of table b with the classes in mask: chunk_steps x [taps + counters, the H
+// pass of each class present, the E pass of each class present]
 cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraphExec_t* out) {
     if (p->graph[b][mask] && p->graph_gen[b][mask] == t.gen) {
         *out = p->graph[b][mask];
@@ -209,15 +220,16 @@ cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraph
         p->graph[b][mask] = nullptr;
     }
     cudaGraph_t gr = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(p->cs, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    for (int s = 0; s < p->chunk; ++s) {
-        k_prologue_pool<float><<<kPoolMaxInst, 256, 0, p->cs>>>(p->d_tab[b]);
-        for (int pass = 0; pass < 2; ++pass)
-            for (int cls = 0; cls < 3; ++cls)
-                if (mask & (1 << cls)) launch_pool_class(t, cls, p->d_tab[b], p->cs, pass == 1);
+    cudaError_t e = cudaGraphCreate(&gr, 0);
+    cudaGraphNode_t prev = nullptr;
+    for (int s = 0; s < p->chunk && e == cudaSuccess; ++s) {
+        e = add_node(gr, &prev, (const void*)k_prologue_pool<float>, kPoolMaxInst, 256, p->d_tab[b]);
+        for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass)
+            for (int cls = 0; cls < 3 && e == cudaSuccess; ++cls)
+                if (mask & (1 << cls))
+                    e = add_node(gr, &prev, pool_pass_func(cls, t.minb[cls], pass == 1),
+                                 pass == 1 ? t.grid_e[cls] : t.grid_h[cls], kPoolTpb, p->d_tab[b]);
     }
-    e = cudaStreamEndCapture(p->cs, &gr);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b][mask], gr, 0);
     if (gr) cudaGraphDestroy(gr);
     if (e == cudaSuccess) {
@@ -348,7 +360,6 @@ void pool_free(FitPool* p) {
         if (p->h_tab[b]) cudaFreeHost(p->h_tab[b]);
     }
     if (p->ps) cudaStreamDestroy(p->ps);
-    if (p->cs) cudaStreamDestroy(p->cs);
     delete p;
 }
 
@@ -377,7 +388,6 @@ int fit_pool_create(int32_t device, int64_t budget_bytes, int32_t chunk_steps, i
     for (int c = 0; c < 3 && e == cudaSuccess; ++c)
         e = pool_grids(p->nsm, c, p->minb[c], ctas_per_sm, &p->grid_h[c], &p->grid_e[c]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->ps, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cs, cudaStreamNonBlocking);
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         e = cudaEventCreateWithFlags(&p->ev[b], cudaEventDisableTiming | cudaEventBlockingSync);
         if (e == cudaSuccess) e = cudaMalloc(&p->d_tab[b], sizeof(PoolTable<float>));

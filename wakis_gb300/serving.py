@@ -323,7 +323,6 @@ class ServingLoop:
     def run(self, requests, time_scale=1.0):
         """Serves the requests (arrival times in seconds, scaled by time_scale) and returns
         per-request records and a summary."""
-        import torch
         tmp = tempfile.mkdtemp()
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         queue = []
@@ -365,7 +364,6 @@ class ServingLoop:
                         self.results[req.tag] = res
                     job.close()
                     del job
-                    torch.cuda.synchronize(self.device)
                     self.pool.release(nbytes)
             elif pending and not queue:
                 time.sleep(max(0.0, pending[0].arrival * time_scale - (time.perf_counter() - t0)))
