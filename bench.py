@@ -206,8 +206,14 @@ def run_ours(args, rank, world):
     N = P.nx * P.ny * P.nz
     mask = P.walls_mask(device=dev)
     grid, wake, s = P.build(wg, mask)
-    if args.variant == "staged":
-        s._ctx.call("fit_set_kernel_variant", 1)
+    s.kernels = args.variant
+    tuned = None
+    if s.kernels == "fused":
+        if args.fused_shape:
+            s._ctx.call("fit_set_fused_shape", *args.fused_shape)
+            tuned = {tuple(args.fused_shape): float("nan")}
+        else:
+            tuned = s.tune_fused()
     del mask
     beam, Nt = s._wake_prepare(wake, P.wakelength, "both")
     vt = s._wake_device_setup(beam, Nt)
@@ -247,6 +253,15 @@ def run_ours(args, rank, world):
     ach_h = BYTES_H * N / (kt[0] / 1e3) / 1e9
     ach_step = BYTES_STEP_MODEL * N / (ms / K / 1e3) / 1e9
     traffic = profile_traffic()
+    fused = None
+    if s.kernels == "fused":
+        kf = np.zeros(1)
+        s._ctx.call("fit_time_fused", 10, nat.dptr(kf))
+        ach_f = BYTES_STEP_MODEL * N / (kf[0] / 1e3) / 1e9
+        fused = {"bound": "hbm", "kernel": "k_step_fused (whole step, lossy, FP32)", "achieved": ach_f, "peak": peak,
+                 "unit": "GB/s", "frac": ach_f / peak, "traffic": profile_traffic("fused_cfg4_ncu.md"),
+                 "algorithmic_bytes_per_launch": BYTES_STEP_MODEL * N, "ms_per_launch": kf[0],
+                 "peak_source": f"{src} HBM copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"}
     out = {"metric": METRIC, "value": value, "unit": "Mcell-updates/s", "n_gpus": world, "steps": K, "warmup": W,
            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (analytic pillbox geometry, Gaussian beam)",
@@ -265,6 +280,17 @@ def run_ours(args, rank, world):
                              "note": "84 B/cell-update = fused-step algorithmic bytes; the two-pass step moves "
                                      "108 B/cell"},
            "gpu_launches": int(launches)}
+    if fused is not None:
+        out["roofline_two_pass_e"] = out["roofline"]
+        out["roofline"] = fused
+        shapes = {k: t for k, t in tuned.items() if k != "two-pass"}
+        best = min(shapes, key=lambda t: shapes[t] if shapes[t] == shapes[t] else 0.0)
+        out["fused_autotune"] = {"best": list(best),
+                                 "ms_per_step": {f"v{v}r{r}z{z}": t for (v, r, z), t in sorted(shapes.items())},
+                                 "two_pass_ms_per_step": tuned.get("two-pass")}
+        out["config"]["kernels"] = "fused single-pass step (ping-pong field buffers)"
+    else:
+        out["config"]["kernels"] = f"{s.kernels} H and E pass kernels"
     csum = clk.summary(dev.index)
     if csum is not None:
         out["clocks"] = csum
@@ -273,7 +299,7 @@ def run_ours(args, rank, world):
     gc.collect()
     torch.cuda.empty_cache()
     if not args.no_e2e:
-        out["e2e"] = e2e(wg, torch, dev, P)
+        out["e2e"] = e2e(wg, torch, dev, P, args.variant)
     if rank == 0 and not args.no_cpu:
         rate, sample, cores = cpu_sample_rate()
         out["cpu_baseline"] = {"value": rate, "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
@@ -282,7 +308,7 @@ def run_ours(args, rank, world):
         print(json.dumps(out), flush=True)
 
 
-def e2e(wg, torch, dev, P):
+def e2e(wg, torch, dev, P, kernels="direct"):
     """Complete wakesolve through the public API: host numpy geometry -> GridFIT3D ->
     SolverFIT3D -> wakesolve -> WP / WPx / WPy / Z / Zx / Zy back on the host."""
     torch.cuda.synchronize()
@@ -290,6 +316,7 @@ def e2e(wg, torch, dev, P):
     h2d = mask.nbytes
     t0 = time.perf_counter()
     grid, wake, s = P.build(wg, mask)
+    s.kernels = kernels
     s.wakesolve(wakelength=P.wakelength)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
@@ -539,9 +566,9 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
-def profile_traffic():
-    """DRAM bytes per E-pass launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "epass_cfg4_ncu.md")
+def profile_traffic(name="epass_cfg4_ncu.md"):
+    """DRAM bytes per launch (scaled to the full grid) from a committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for ln in open(p):
@@ -572,8 +599,11 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-no-fp64", action="store_true")
     ap.add_argument("--serve-no-saturated", action="store_true")
-    ap.add_argument("--variant", default="direct", choices=["staged", "direct"],
-                    help="pass kernels: direct-load kernels (default) or the persistent bulk-copy staged kernels")
+    ap.add_argument("--fused-shape", type=int, nargs=3, default=None, metavar=("VEC", "ROWS", "ZSEG"),
+                    help="fused step tile shape (skips the autotuner)")
+    ap.add_argument("--variant", default="auto", choices=["auto", "staged", "direct", "fused"],
+                    help="step kernels: auto (the solver default: fused where it applies), direct H/E pass kernels, "
+                         "persistent bulk-copy staged pass kernels, or the fused single-pass step")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -199,9 +199,24 @@ FIT_API int fit_dft_noalloc(const double *x, int32_t nsig, int64_t len, int64_t 
  * then returned without completing its pass).  The word is cleared by the read. */
 FIT_API int fit_check_error(FitCtx *ctx);
 
-/* Chooses the pass kernels: staged != 0 uses the persistent bulk-copy kernels when
- * Nx*sizeof(dtype) is a multiple of 16 bytes; 0 (the default) uses the direct kernels. */
-FIT_API int fit_set_kernel_variant(FitCtx *ctx, int32_t staged);
+/* Chooses the step kernels.  0 (the default): the direct H and E pass kernels.
+ * 1: the persistent bulk-copy (staged) pass kernels when Nx*sizeof(dtype) is a multiple
+ * of 16 bytes.  2: fit_run takes its steps with the fused single-pass kernel (each value
+ * read and written once per step) between the caller's E, H and a second pair of field
+ * buffers the library allocates (3*N elements each); pairs of steps end in the caller's
+ * buffers, and a single step, plane sources, low-face ABC updates, explicit J and grids
+ * with Nx not a multiple of 2 use the pass kernels. */
+FIT_API int fit_set_kernel_variant(FitCtx *ctx, int32_t variant);
+/* Tile shape of the fused step: vec cells per thread along x (2, or 4 for FP32; Nx must
+ * be a multiple), rows (4 or 8) rows of 32 threads per CTA, zseg z ranges per tile
+ * column (1..Nz).  fit_set_kernel_variant(ctx, 2) sets a default; the solver's
+ * autotuner times the candidates on the grid itself with fit_time_fused. */
+FIT_API int fit_set_fused_shape(FitCtx *ctx, int32_t vec, int32_t rows, int32_t zseg);
+/* Times, beam off, on the context stream between CUDA events: reps fused steps from
+ * (E, H) into the second buffers (ms_out[0]), and reps two-pass steps (H pass + E pass)
+ * in place on copies of E and H in the second buffers (ms_out[1]); average milliseconds
+ * per step.  E, H and J are not changed.  The solver's autotuner compares the two. */
+FIT_API int fit_time_fused(FitCtx *ctx, int32_t reps, double *ms_out);
 
 /* Benchmark support: launches the H pass reps times, then the elided-J E pass reps
  * times (advancing the fields), on the context's stream between CUDA events; ms_out

@@ -1,0 +1,87 @@
+"""Fused single-pass step kernel (SolverFIT3D.kernels = 'fused'): the device loop with
+ping-pong field buffers must give the two-pass results to rounding, including the row
+crossings of periodic faces, partial tiles, several z ranges per tile column and odd
+step counts, and must pass the reference fixtures with the parity tolerances.
+
+The per-cell code is the two-pass code, but the compiler contracts multiply-adds of the
+inlined copies independently, so results agree to the last bits rather than bit for
+bit: relative L2 differences below 1e-12 (FP64) and 1e-5 (FP32) are required; a wrong
+halo or crossing would differ at order one."""
+
+import numpy as np
+import pytest
+import torch
+
+import cases as C
+from oracle_runner import load_golden, rel_l2
+from product_runner import run_case
+
+pytestmark = pytest.mark.gpu
+
+FUSED_CASES = ["cavity_f64", "lossy_f64", "lossy_f32", "longitudinal_f64", "skip_nonuniform_f64",
+               "periodic_cond_f32"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def _run(name, kernels, tmp_path, monkeypatch):
+    monkeypatch.setenv("WAKIS_GB300_KERNELS", kernels)
+    return run_case(name, tmpdir=tmp_path)
+
+
+@pytest.mark.parametrize("name", FUSED_CASES)
+def test_fused_equals_two_pass(name, tmp_path, monkeypatch):
+    fused = _run(name, "fused", tmp_path, monkeypatch)
+    direct = _run(name, "direct", tmp_path, monkeypatch)
+    f64 = C.CASES[name]["dtype"] == "float64"
+    for k, v in direct.items():
+        if k in ("s", "f", "dt", "Nt"):
+            np.testing.assert_array_equal(np.asarray(fused[k]), np.asarray(v), err_msg=f"{name}:{k}")
+        else:
+            assert close(fused[k], v, f64), (name, k, rel_l2(fused[k], v))
+    g = load_golden(name)
+    tol = 1e-10 if f64 else 1e-4
+    for k in ("WP", "Z"):
+        if k in g:
+            assert rel_l2(fused[k], g[k]) < tol, (k, rel_l2(fused[k], g[k]))
+
+
+@pytest.mark.parametrize("bcs,steps", [
+    ((["pmc", "periodic", "pec"], ["pec", "periodic", "pml"]), 7),
+    ((["periodic", "periodic", "periodic"], ["periodic", "periodic", "periodic"]), 130),
+    ((["pec", "pmc", "pec"], ["pml", "pec", "pmc"]), 66),
+])
+def test_fused_random_fields_all_face_kinds(bcs, steps):
+    """Random E, H on a 16 x 12 x 40 grid (a partial tile in x and y; five z ranges per
+    tile column), lossy blocks, faces of every kind the fused step serves: the fused
+    device loop equals the two-pass device loop to rounding."""
+    import wakis_gb300 as wg
+    x = np.linspace(-1, 1, 17)
+    y = np.linspace(-0.8, 0.7, 13)
+    z = np.linspace(-2, 2, 41)
+    out = {}
+    for kernels in ("direct", "fused"):
+        blk = lambda X, Y, Z: (np.abs(X) < 0.4) & (Z > 0.3) & (Z < 1.1)
+        grid = wg.GridFIT3D(x=x, y=y, z=z, stl_solids={"blk": blk}, stl_materials={"blk": [2.0, 1.0, 50.0]},
+                            verbose=0)
+        s = wg.SolverFIT3D(grid, cfln=0.5, bc_low=bcs[0], bc_high=bcs[1], use_stl=True, bg=[1.0, 1.0],
+                           dtype=np.float32, n_pml=4, verbose=0)
+        s.kernels = kernels
+        rng = np.random.default_rng(5)
+        s.E.fromarray(rng.standard_normal((s.Nx, s.Ny, s.Nz, 3)).astype(np.float32))
+        s.H.fromarray(rng.standard_normal((s.Nx, s.Ny, s.Nz, 3)).astype(np.float32))
+        s.emsolve(steps)
+        out[kernels] = (s.E.numpy(), s.H.numpy(), s.J.numpy())
+    for a, b, k in zip(out["fused"], out["direct"], "EHJ"):
+        assert close(a, b, False), (k, rel_l2(a, b))
+
+
+def close(a, b, f64):
+    a, b = np.asarray(a), np.asarray(b)
+    if not np.any(b):
+        return not np.any(a)
+    return rel_l2(a, b) < (1e-12 if f64 else 1e-5)

@@ -1,6 +1,7 @@
 """Serving pool on the GPU: pooled solves give the same results as the plain public API
-(bit for bit: the per-cell arithmetic is the same code), alone or in a mix, under a
-budget that admits one at a time or all at once; contexts are locked while pooled."""
+with the two-pass kernels (bit for bit: the per-cell arithmetic is the same code), alone
+or in a mix, under a budget that admits one at a time or all at once; contexts are
+locked while pooled.  Against the default (fused) wakesolve they agree to rounding."""
 
 import numpy as np
 import pytest
@@ -30,7 +31,7 @@ def small_requests():
 
 @pytest.fixture(scope="module")
 def alone():
-    return {r.tag: S.solve_alone(r, np.float32) for r in small_requests()}
+    return {r.tag: S.solve_alone(r, np.float32, kernels="direct") for r in small_requests()}
 
 
 def assert_same(got, ref):
@@ -48,6 +49,24 @@ def test_pooled_mix_matches_wakesolve(alone):
     for tag, ref in alone.items():
         assert_same(loop.results[tag], ref)
     assert {r["tag"]: r["steps"] for r in recs} == {t: alone[t]["Nt"] for t in alone}
+
+
+def test_pooled_results_match_the_default_wakesolve_to_rounding():
+    for req in small_requests()[:2]:
+        ref = S.solve_alone(req, np.float32)  # default kernels (fused where it applies)
+        pool = nat.Pool(1 << 30, chunk_steps=32)
+        job = S.ServedSolve(req)
+        try:
+            job.submit(pool)
+            while not pool.poll(wait_ms=100):
+                pass
+            got = job.finish()
+        finally:
+            pool.close()
+            job.close()
+        for k in ("WP", "Z"):
+            a, b = np.asarray(got[k]), np.asarray(ref[k])
+            assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b), k
 
 
 def test_solves_submitted_together_share_chunks(alone):

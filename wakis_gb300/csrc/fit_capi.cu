@@ -84,6 +84,10 @@ struct FitCtx {
     int* d_err = nullptr;   // device error word written by kernels (FIT_ERR_TIMEOUT)
     int nsm = 1;            // SM count: grid of the persistent staged kernels
     bool staged = false;    // staged (bulk-copy) passes when the grid is aligned (opt-in)
+    bool fused = false;     // fused single-pass step in device loops (ping-pong with E2/H2)
+    void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
+    int fused_vec = 4, fused_rows = 8, fused_zseg = 1;  // tile shape of the fused step
+    bool graph_fused = false;  // the cached graph holds fused steps
     std::atomic<bool> in_pool{false};  // submitted to a FitPool and not yet reported done
     std::string err;
 };
@@ -327,6 +331,88 @@ void launch_step(FitCtx* c, long long n, int mode, bool device_step) {
         launch_step_t<float>(c, n, mode, device_step);
 }
 
+// the fused step serves the elided-J device loop without plane sources or ABC updates,
+// on grids with Nx a multiple of the 2- or 4-wide vector
+bool fused_ok(const FitCtx* c, int mode) {
+    return c->fused && c->E2 && c->H2 && mode != 2 && !c->plane.active && !c->abc_axes && pick_vec(c) >= 2;
+}
+
+template <typename T, int VEC, int FY>
+void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
+    constexpr int FX = 32 * VEC;
+    const T* Ein = static_cast<const T*>(forward ? c->E : c->E2);
+    const T* Hin = static_cast<const T*>(forward ? c->H : c->H2);
+    T* Eout = static_cast<T*>(forward ? c->E2 : c->E);
+    T* Hout = static_cast<T*>(forward ? c->H2 : c->H);
+    const int zlen = (c->g.nz + c->fused_zseg - 1) / c->fused_zseg;
+    const dim3 grid((unsigned)((c->g.nx + FX - 1) / FX), (unsigned)((c->g.ny + FY - 1) / FY),
+                    (unsigned)((c->g.nz + zlen - 1) / zlen));
+    const dim3 block(32, FY + 1);
+    const T* ch = static_cast<const T*>(c->ch);
+    const T* ce = static_cast<const T*>(c->ce);
+    const T* cl = static_cast<const T*>(c->cl);
+    T* J = static_cast<T*>(c->J);
+    if (mode == 1)
+        k_step_fused<T, VEC, FY, 1><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g,
+                                                              metric<T>(c), beam, st, zlen);
+    else
+        k_step_fused<T, VEC, FY, 0><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g,
+                                                              metric<T>(c), beam, st, zlen);
+    count(c);
+}
+
+// the fused step in the context's tile shape (fused_vec cells per thread, fused_rows rows)
+void launch_fused(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
+    const bool r8 = c->fused_rows == 8;
+    if (c->dtype == FIT_F64) {
+        r8 ? launch_fused_shape<double, 2, 8>(c, mode, st, forward, beam)
+           : launch_fused_shape<double, 2, 4>(c, mode, st, forward, beam);
+    } else if (c->fused_vec == 4) {
+        r8 ? launch_fused_shape<float, 4, 8>(c, mode, st, forward, beam)
+           : launch_fused_shape<float, 4, 4>(c, mode, st, forward, beam);
+    } else {
+        r8 ? launch_fused_shape<float, 2, 8>(c, mode, st, forward, beam)
+           : launch_fused_shape<float, 2, 4>(c, mode, st, forward, beam);
+    }
+}
+
+// default tile shape: the widest vector, 8 rows, z ranges for about four waves
+void fused_default_shape(FitCtx* c) {
+    c->fused_vec = pick_vec(c) == 4 ? 4 : 2;
+    c->fused_rows = 8;
+    const long long tiles = (long long)((c->g.nx + 32 * c->fused_vec - 1) / (32 * c->fused_vec)) *
+                            ((c->g.ny + c->fused_rows - 1) / c->fused_rows);
+    const long long want = (4LL * 2 * c->nsm + tiles - 1) / tiles;
+    c->fused_zseg = (int)std::max<long long>(1, std::min<long long>(want, std::max(1, c->g.nz / 8)));
+}
+
+// one fused step: (E, H) -> (E2, H2) when forward, else back; the prologue (wake taps,
+// step counter) reads the step's input buffer
+void launch_fused_step(FitCtx* c, int mode, bool forward, const StepArgs& st, long long n) {
+    const bool dev = st.d_step != nullptr;
+    if (c->dtype == FIT_F64) {
+        k_prologue<double><<<1, 512, 0, c->own>>>(static_cast<double*>(forward ? c->E : c->E2),
+                                                   static_cast<double*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
+                                                   n, dev ? c->d_step : nullptr);
+        count(c);
+        launch_fused(c, mode, st, forward, c->beam);
+    } else {
+        k_prologue<float><<<1, 512, 0, c->own>>>(static_cast<float*>(forward ? c->E : c->E2),
+                                                 static_cast<float*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
+                                                 n, dev ? c->d_step : nullptr);
+        count(c);
+        launch_fused(c, mode, st, forward, c->beam);
+    }
+}
+
+StepArgs device_step_args(const FitCtx* c) {
+    StepArgs st{};
+    st.d_step = c->d_step;
+    st.vt_table = c->d_vt_table;
+    st.vt_len = c->vt_len;
+    return st;
+}
+
 int check_ready(FitCtx* c) {
     if (!c) return FIT_ERR_ARG;
     if (!c->metrics_set) return fail(c, FIT_ERR_STATE, "fit_set_metrics has not been called");
@@ -435,7 +521,7 @@ int fit_ctx_destroy(FitCtx* c) {
         dfree(c->tL_T[a], c->own);
         dfree(c->L_T[a], c->own);
     }
-    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg}) dfree(p, c->own);
+    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg, c->E2, c->H2}) dfree(p, c->own);
     for (void* p : {(void*)c->d_beam_z, (void*)c->d_beam_dtieps, (void*)c->d_vt_table, (void*)c->d_prof,
                     (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
                     (void*)c->d_em, (void*)c->d_ek0, (void*)c->d_ecnt, (void*)c->d_dz, (void*)c->d_acc,
@@ -813,8 +899,46 @@ int fit_run(FitCtx* c, int64_t n0, int64_t nsteps) {
     CK(cudaMemcpyAsync(c->d_step, &host_n0, sizeof(long long), cudaMemcpyHostToDevice, c->own));
     CK(cudaStreamSynchronize(c->own));
     const long long chunk = 64;
+    if (fused_ok(c, mode)) {
+        // pairs of fused steps leave the state in the caller's buffers; an odd count
+        // takes its first step with the in-place two-pass kernels
+        const StepArgs st = device_step_args(c);
+        long long done = 0;
+        if (nsteps % 2) {
+            launch_step(c, 0, mode, true);
+            done = 1;
+        }
+        if (nsteps - done >= chunk && (!c->graph || c->graph_chunk != chunk || !c->graph_fused)) {
+            invalidate(c);
+            cudaGraph_t gr;
+            CK(cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal));
+            c->capturing = true;
+            for (long long s = 0; s < chunk; s += 2) {
+                launch_fused_step(c, mode, true, st, 0);
+                launch_fused_step(c, mode, false, st, 0);
+            }
+            c->capturing = false;
+            cudaError_t e = cudaStreamEndCapture(c->own, &gr);
+            if (e != cudaSuccess) return fail(c, FIT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&c->graph, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e != cudaSuccess) return fail(c, FIT_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+            c->graph_chunk = chunk;
+            c->graph_fused = true;
+        }
+        while (nsteps - done >= chunk) {
+            CK(cudaGraphLaunch(c->graph, c->own));
+            g_launches += chunk * 2;
+            done += chunk;
+        }
+        for (; done < nsteps; done += 2) {
+            launch_fused_step(c, mode, true, st, 0);
+            launch_fused_step(c, mode, false, st, 0);
+        }
+        return leave(c);
+    }
     if (nsteps >= chunk) {
-        if (!c->graph || c->graph_chunk != chunk) {
+        if (!c->graph || c->graph_chunk != chunk || c->graph_fused) {
             if (c->graph) {
                 cudaGraphExecDestroy(c->graph);
                 c->graph = nullptr;
@@ -830,6 +954,7 @@ int fit_run(FitCtx* c, int64_t n0, int64_t nsteps) {
             cudaGraphDestroy(gr);
             if (e != cudaSuccess) return fail(c, FIT_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
             c->graph_chunk = chunk;
+            c->graph_fused = false;
         }
     }
     long long done = 0;
@@ -996,12 +1121,96 @@ int fit_check_error(FitCtx* c) {
     return FIT_OK;
 }
 
-int fit_set_kernel_variant(FitCtx* c, int32_t staged) {
+int fit_set_kernel_variant(FitCtx* c, int32_t variant) {
     if (!c) return FIT_ERR_ARG;
     if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    if (variant < 0 || variant > 2) return fail(c, FIT_ERR_ARG, "variant must be 0 (direct), 1 (staged) or 2 (fused)");
     invalidate(c);
-    c->staged = staged != 0;
+    c->staged = variant == 1;
+    c->fused = variant == 2;
+    if (c->fused && !c->E2) {
+        const size_t fb = 3 * (size_t)c->g.N * esize(c);
+        int rc = dev_alloc(c, &c->E2, fb);
+        if (!rc) rc = dev_alloc(c, &c->H2, fb);
+        if (rc) {
+            c->fused = false;
+            return rc;
+        }
+        fused_default_shape(c);
+    }
     return FIT_OK;
+}
+
+int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    const bool vec_ok = (vec == 2 && c->g.nx % 2 == 0) || (vec == 4 && c->dtype == FIT_F32 && c->g.nx % 4 == 0);
+    if (!vec_ok || (rows != 4 && rows != 8) || zseg < 1 || zseg > c->g.nz)
+        return fail(c, FIT_ERR_ARG, "bad fused tile shape (vec %d, rows %d, z ranges %d)", vec, rows, zseg);
+    invalidate(c);
+    c->fused_vec = vec;
+    c->fused_rows = rows;
+    c->fused_zseg = zseg;
+    return FIT_OK;
+}
+
+int fit_time_fused(FitCtx* c, int32_t reps, double* ms_out) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (reps < 1 || !ms_out) return fail(c, FIT_ERR_ARG, "bad timing arguments");
+    const int mode = c->use_cond ? 1 : 0;
+    if (!fused_ok(c, mode)) return fail(c, FIT_ERR_STATE, "the fused step is not enabled for this context");
+    rc = enter(c);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    StepArgs st{};
+    BeamArgs nobeam = c->beam;
+    nobeam.active = 0;
+    launch_fused(c, mode, st, true, nobeam);  // warm-up
+    CK(cudaEventRecord(e0, c->own));
+    for (int r = 0; r < reps; ++r) launch_fused(c, mode, st, true, nobeam);
+    CK(cudaEventRecord(e1, c->own));
+    CK(cudaEventSynchronize(e1));
+    float a = 0.f;
+    CK(cudaEventElapsedTime(&a, e0, e1));
+    ms_out[0] = a / reps;
+    // the two-pass step, in place on copies of the fields in the second buffers
+    const size_t fb = 3 * (size_t)c->g.N * esize(c);
+    CK(cudaMemcpyAsync(c->E2, c->E, fb, cudaMemcpyDeviceToDevice, c->own));
+    CK(cudaMemcpyAsync(c->H2, c->H, fb, cudaMemcpyDeviceToDevice, c->own));
+    std::swap(c->E, c->E2);
+    std::swap(c->H, c->H2);
+    const int saved = c->beam.active;
+    c->beam.active = 0;
+    const int vec = pick_vec(c);
+    auto pass_pair = [&]() {
+        if (c->dtype == FIT_F64) {
+            launch_h<double, 2>(c);
+            launch_e<double, 2>(c, mode, st);
+        } else if (vec == 4) {
+            launch_h<float, 4>(c);
+            launch_e<float, 4>(c, mode, st);
+        } else {
+            launch_h<float, 2>(c);
+            launch_e<float, 2>(c, mode, st);
+        }
+    };
+    pass_pair();  // warm-up
+    cudaEventRecord(e0, c->own);
+    for (int r = 0; r < reps; ++r) pass_pair();
+    cudaEventRecord(e1, c->own);
+    cudaError_t err = cudaEventSynchronize(e1);
+    std::swap(c->E, c->E2);
+    std::swap(c->H, c->H2);
+    c->beam.active = saved;
+    if (err != cudaSuccess) return fail(c, FIT_ERR_CUDA, "fit_time_fused: %s", cudaGetErrorString(err));
+    CK(cudaEventElapsedTime(&a, e0, e1));
+    ms_out[1] = a / reps;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return leave(c);
 }
 
 int fit_version(char* buf, int64_t len) {

@@ -448,12 +448,12 @@ __device__ __forceinline__ void cell_of(long long n, const Geom& g, int& i0, int
 // ---------------------------------------------------------------- direct kernels
 // One thread per VEC cells, inputs loaded straight from global memory.  Used for grids
 // whose Nx is not a multiple of the 16-byte vector width and for the explicit-J pass.
-// H pass of the VEC cells starting at component-local flat index n
+// New H of the VEC cells starting at component-local flat index n (cell (i0, j, k)),
+// from E and the old H: the values land in hx, hy, hz; nothing is stored.
 template <typename T, int VEC>
-__device__ __forceinline__ void hpass_at(const T* __restrict__ E, T* __restrict__ H, const T* __restrict__ ch,
-                                         const Geom& g, const Metric<T>& mt, long long n) {
-    int i0, j, k;
-    cell_of(n, g, i0, j, k);
+__device__ __forceinline__ void hpass_eval(const T* __restrict__ E, const T* H, const T* __restrict__ ch,
+                                           const Geom& g, const Metric<T>& mt, long long n, int i0, int j, int k,
+                                           T (&hx)[VEC], T (&hy)[VEC], T (&hz)[VEC]) {
     const T* Ex = E;
     const T* Ey = E + g.N;
     const T* Ez = E + 2 * g.N;
@@ -483,7 +483,7 @@ __device__ __forceinline__ void hpass_at(const T* __restrict__ E, T* __restrict_
         eyx = __ldg(Ey + n + VEC);
         ezx = __ldg(Ez + n + VEC);
     }
-    T hx[VEC], hy[VEC], hz[VEC], cx[VEC], cy[VEC], cz[VEC];
+    T cx[VEC], cy[VEC], cz[VEC];
     ld_v<T, VEC>(hx, H + n);
     ld_v<T, VEC>(hy, H + g.N + n);
     ld_v<T, VEC>(hz, H + 2 * g.N + n);
@@ -491,6 +491,16 @@ __device__ __forceinline__ void hpass_at(const T* __restrict__ E, T* __restrict_
     ldg_v<T, VEC>(cy, ch + g.N + n);
     ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
     hpass_cells<T, VEC>(ex, ey, ez, exy, ezy, exz, eyz, eyx, ezx, hx, hy, hz, cx, cy, cz, i0, j, k, g, mt);
+}
+
+// H pass of the VEC cells starting at component-local flat index n
+template <typename T, int VEC>
+__device__ __forceinline__ void hpass_at(const T* __restrict__ E, T* __restrict__ H, const T* __restrict__ ch,
+                                         const Geom& g, const Metric<T>& mt, long long n) {
+    int i0, j, k;
+    cell_of(n, g, i0, j, k);
+    T hx[VEC], hy[VEC], hz[VEC];
+    hpass_eval<T, VEC>(E, H, ch, g, mt, n, i0, j, k, hx, hy, hz);
     st_v<T, VEC>(H + n, hx);
     st_v<T, VEC>(H + g.N + n, hy);
     st_v<T, VEC>(H + 2 * g.N + n, hz);
@@ -508,48 +518,25 @@ __global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __
 // MODE 1: E = cl*E + ce*(C^T ĥ)                 (J = sigma*E_prev folded into cl)
 // MODE 2: E = E + ce*(C^T ĥ) - cj*J; J = sg*E   (explicit J; J written if conductive)
 // The beam line (ixs, iys, :) of the z component uses the beam current instead of J.
+// E update of the VEC cells at flat index n (cell (i0, j, k)) from the new H around
+// them: own (hx, hy, hz), the row below (hxy, hzy at n - Nx), the plane below (hxz, hyz
+// at n - Nx*Ny) and the value before the vector along x (hyx, hzx at n - 1).  E is read
+// from Esrc and written to Edst (the same array for the in-place passes).
 template <typename T, int VEC, int MODE>
-__device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict__ H, const T* __restrict__ ce,
-                                         const T* __restrict__ cl, T* __restrict__ J, const T* __restrict__ cj,
-                                         const T* __restrict__ sg, int use_cond, const Geom& g, const Metric<T>& mt,
-                                         const BeamArgs& b, const PlaneArgs& pl, const StepArgs& st, long long n) {
-    int i0, j, k;
-    cell_of(n, g, i0, j, k);
-    const T* Hx = H;
-    const T* Hy = H + g.N;
-    const T* Hz = H + 2 * g.N;
-    T hx[VEC], hy[VEC], hz[VEC];
-    ldg_v<T, VEC>(hx, Hx + n);
-    ldg_v<T, VEC>(hy, Hy + n);
-    ldg_v<T, VEC>(hz, Hz + n);
-    const bool yv = (j > 0) || (k > 0);
-    const bool zv = (k > 0);
-    T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
-    if (yv) {
-        ldg_v<T, VEC>(hxy, Hx + n - g.sy);
-        ldg_v<T, VEC>(hzy, Hz + n - g.sy);
-    } else {
-        zero_v<T, VEC>(hxy);
-        zero_v<T, VEC>(hzy);
-    }
-    if (zv) {
-        ldg_v<T, VEC>(hxz, Hx + n - g.sz);
-        ldg_v<T, VEC>(hyz, Hy + n - g.sz);
-    } else {
-        zero_v<T, VEC>(hxz);
-        zero_v<T, VEC>(hyz);
-    }
-    T hyx = T(0), hzx = T(0);
-    if (n > 0) {
-        hyx = __ldg(Hy + n - 1);
-        hzx = __ldg(Hz + n - 1);
-    }
+__device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&hx)[VEC], const T (&hy)[VEC],
+                                             const T (&hz)[VEC], const T (&hxy)[VEC], const T (&hzy)[VEC],
+                                             const T (&hxz)[VEC], const T (&hyz)[VEC], T hyx, T hzx,
+                                             const T* __restrict__ ce, const T* __restrict__ cl, T* __restrict__ J,
+                                             const T* __restrict__ cj, const T* __restrict__ sg, int use_cond,
+                                             const Geom& g, const Metric<T>& mt, const BeamArgs& b,
+                                             const PlaneArgs& pl, const StepArgs& st, long long n, int i0, int j,
+                                             int k) {
     T cur[3][VEC];
     epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
     T ex[VEC], ey[VEC], ez[VEC], kx[VEC], ky[VEC], kz[VEC];
-    ld_v<T, VEC>(ex, E + n);
-    ld_v<T, VEC>(ey, E + g.N + n);
-    ld_v<T, VEC>(ez, E + 2 * g.N + n);
+    ld_v<T, VEC>(ex, Esrc + n);
+    ld_v<T, VEC>(ey, Esrc + g.N + n);
+    ld_v<T, VEC>(ez, Esrc + 2 * g.N + n);
     ldg_v<T, VEC>(kx, ce + n);
     ldg_v<T, VEC>(ky, ce + g.N + n);
     ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
@@ -610,9 +597,50 @@ __device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict_
         }
         epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, J, n, i0, j, k, use_cond, g, b, pl, st);
     }
-    st_v<T, VEC>(E + n, ex);
-    st_v<T, VEC>(E + g.N + n, ey);
-    st_v<T, VEC>(E + 2 * g.N + n, ez);
+    st_v<T, VEC>(Edst + n, ex);
+    st_v<T, VEC>(Edst + g.N + n, ey);
+    st_v<T, VEC>(Edst + 2 * g.N + n, ez);
+}
+
+
+template <typename T, int VEC, int MODE>
+__device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict__ H, const T* __restrict__ ce,
+                                         const T* __restrict__ cl, T* __restrict__ J, const T* __restrict__ cj,
+                                         const T* __restrict__ sg, int use_cond, const Geom& g, const Metric<T>& mt,
+                                         const BeamArgs& b, const PlaneArgs& pl, const StepArgs& st, long long n) {
+    int i0, j, k;
+    cell_of(n, g, i0, j, k);
+    const T* Hx = H;
+    const T* Hy = H + g.N;
+    const T* Hz = H + 2 * g.N;
+    T hx[VEC], hy[VEC], hz[VEC];
+    ldg_v<T, VEC>(hx, Hx + n);
+    ldg_v<T, VEC>(hy, Hy + n);
+    ldg_v<T, VEC>(hz, Hz + n);
+    const bool yv = (j > 0) || (k > 0);
+    const bool zv = (k > 0);
+    T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
+    if (yv) {
+        ldg_v<T, VEC>(hxy, Hx + n - g.sy);
+        ldg_v<T, VEC>(hzy, Hz + n - g.sy);
+    } else {
+        zero_v<T, VEC>(hxy);
+        zero_v<T, VEC>(hzy);
+    }
+    if (zv) {
+        ldg_v<T, VEC>(hxz, Hx + n - g.sz);
+        ldg_v<T, VEC>(hyz, Hy + n - g.sz);
+    } else {
+        zero_v<T, VEC>(hxz);
+        zero_v<T, VEC>(hyz);
+    }
+    T hyx = T(0), hzx = T(0);
+    if (n > 0) {
+        hyx = __ldg(Hy + n - 1);
+        hzx = __ldg(Hz + n - 1);
+    }
+    epass_finish<T, VEC, MODE>(E, E, hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, ce, cl, J, cj, sg, use_cond, g, mt, b,
+                               pl, st, n, i0, j, k);
 }
 
 template <typename T, int VEC, int MODE>
@@ -624,6 +652,165 @@ __global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.N / VEC) return;
     epass_at<T, VEC, MODE>(E, H, ce, cl, J, cj, sg, use_cond, g, mt, b, pl, st, v * VEC);
+}
+
+// ---------------------------------------------------------------- fused step (2.5-D)
+// One launch takes a whole leapfrog step and touches each value once: E^n and H^(n-1/2)
+// are read from (Ein, Hin), E^(n+1) and H^(n+1/2) written to (Eout, Hout).  With
+// separate input and output buffers every read of an old value is safe wherever the
+// other CTAs are, so no CTA waits for another.  A CTA owns a tile of FX = 32*VEC cells
+// along x and FY rows along y (one warp per row) plus one halo warp, and marches
+// through a range of z planes.  For plane k
+//   1. the row warps compute the new H of the tile (hpass_eval, the code of the
+//      two-pass H kernel) and store it to Hout and to a shared plane buffer; the halo
+//      warp computes, from the old fields, the new H of the row below the tile (flat
+//      index n - Nx) and of the cell before each row segment (n - 1): the values the E
+//      update needs from outside the tile.  Neighbours are flat-index neighbours, so the
+//      row crossings of the reference's curl matrix are kept;
+//   2. after one barrier the row warps update E of the tile from the shared planes k
+//      and k-1 (epass_curl + epass_update, the code of the two-pass E kernel; the
+//      coefficients ce, cl were loaded before the H update) and store it to Eout.
+// Three plane buffers rotate: a buffer is rewritten two planes after its last read, so
+// one barrier per plane suffices.  A CTA whose z range starts at k0 > 0 first computes
+// the new H of plane k0-1 for its tile (not stored to Hout: the CTA below owns it).
+// Per cell the step moves the fused algorithmic bytes (E, H read and written once; ch,
+// ce and cl read once); halo reads of the neighbouring tiles hit L2.
+template <typename T, int VEC, int FY>
+struct FusedShared {
+    T h[3][3][FY + 1][32 * VEC];  // [plane buffer][component][row + 1 (row 0: below the tile)][x]
+    T hx1[3][2][FY + 1];          // [plane buffer][Hy, Hz][row + 1]: the cell before each row segment
+};
+
+template <int FY>
+constexpr int fused_min_blocks() { return FY >= 8 ? 2 : 3; }
+
+template <typename T, int VEC, int FY, int MODE>
+__global__ void __launch_bounds__(32 * (FY + 1), fused_min_blocks<FY>())
+    k_step_fused(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout, T* __restrict__ Hout,
+                 const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl, T* __restrict__ J,
+                 int use_cond, Geom g, Metric<T> mt, BeamArgs b, StepArgs st, int zlen) {
+    constexpr int FX = 32 * VEC;
+    __shared__ FusedShared<T, VEC, FY> sm;
+    const int lane = threadIdx.x, ty = threadIdx.y;
+    const bool halo = ty == FY;  // the halo warp
+    const int i0 = blockIdx.x * FX + lane * VEC;
+    const int jt = blockIdx.y * FY;           // first row of the tile
+    const int j = halo ? jt : jt + ty;        // the halo warp works below row jt
+    const bool on = i0 < g.nx && j < g.ny;
+    const int k0 = blockIdx.z * zlen;
+    const int k1 = min(g.nz, k0 + zlen);
+    const PlaneArgs pl{};
+    const int xo = lane * VEC;
+    if (k0 > 0 && on && !halo) {  // new H of plane k0-1 (the plane below the range) for the tile
+        T hx[VEC], hy[VEC], hz[VEC];
+        const long long n = (long long)i0 + g.sy * j + g.sz * (k0 - 1);
+        hpass_eval<T, VEC>(Ein, Hin, ch, g, mt, n, i0, j, k0 - 1, hx, hy, hz);
+        const int bp = (k0 - 1) % 3;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            sm.h[bp][0][ty + 1][xo + e] = hx[e];
+            sm.h[bp][1][ty + 1][xo + e] = hy[e];
+            sm.h[bp][2][ty + 1][xo + e] = hz[e];
+        }
+    }
+    for (int k = k0; k < k1; ++k) {
+        const int bc = k % 3, bp = (k + 2) % 3;
+        const long long n = (long long)i0 + g.sy * j + g.sz * k;
+        T hx[VEC], hy[VEC], hz[VEC];
+        T kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
+        if constexpr (MODE != 1) {
+            zero_v<T, VEC>(lx);
+            zero_v<T, VEC>(ly);
+            zero_v<T, VEC>(lz);
+        }
+        if (halo) {
+            if (on) {  // the row below the tile: flat n - Nx (may wrap to plane k-1)
+                T ax[VEC], ay[VEC], az[VEC];
+                const long long m = n - g.sy;
+                if (m >= 0) {
+                    int mi, mj, mk;
+                    cell_of(m, g, mi, mj, mk);
+                    hpass_eval<T, VEC>(Ein, Hin, ch, g, mt, m, mi, mj, mk, ax, ay, az);
+                } else {
+                    zero_v<T, VEC>(ax);
+                    zero_v<T, VEC>(az);
+                }
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) {
+                    sm.h[bc][0][0][xo + e] = ax[e];
+                    sm.h[bc][2][0][xo + e] = az[e];
+                }
+            }
+            // the cell before each row segment: flat n - 1 (may wrap)
+            const int ib = blockIdx.x * FX;
+            if (lane < FY && ib < g.nx && jt + lane < g.ny) {
+                const long long m = (long long)ib + g.sy * (jt + lane) + g.sz * k - 1;
+                T ax[1], ay[1], az[1];
+                if (m >= 0) {
+                    int mi, mj, mk;
+                    cell_of(m, g, mi, mj, mk);
+                    hpass_eval<T, 1>(Ein, Hin, ch, g, mt, m, mi, mj, mk, ax, ay, az);
+                } else {
+                    ay[0] = T(0);
+                    az[0] = T(0);
+                }
+                sm.hx1[bc][0][lane + 1] = ay[0];
+                sm.hx1[bc][1][lane + 1] = az[0];
+            }
+        } else if (on) {
+            // the E update's coefficients do not depend on the new H: load them first so
+            // their latency overlaps the H update and the barrier
+            ldg_v<T, VEC>(kx, ce + n);
+            ldg_v<T, VEC>(ky, ce + g.N + n);
+            ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+            if constexpr (MODE == 1) {
+                ldg_v<T, VEC>(lx, cl + n);
+                ldg_v<T, VEC>(ly, cl + g.N + n);
+                ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+            }
+            hpass_eval<T, VEC>(Ein, Hin, ch, g, mt, n, i0, j, k, hx, hy, hz);
+            st_v<T, VEC>(Hout + n, hx);
+            st_v<T, VEC>(Hout + g.N + n, hy);
+            st_v<T, VEC>(Hout + 2 * g.N + n, hz);
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                sm.h[bc][0][ty + 1][xo + e] = hx[e];
+                sm.h[bc][1][ty + 1][xo + e] = hy[e];
+                sm.h[bc][2][ty + 1][xo + e] = hz[e];
+            }
+        }
+        __syncthreads();
+        if (on && !halo) {
+            T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                hxy[e] = sm.h[bc][0][ty][xo + e];
+                hzy[e] = sm.h[bc][2][ty][xo + e];
+            }
+            if (k > 0) {
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) {
+                    hxz[e] = sm.h[bp][0][ty + 1][xo + e];
+                    hyz[e] = sm.h[bp][1][ty + 1][xo + e];
+                }
+            } else {
+                zero_v<T, VEC>(hxz);
+                zero_v<T, VEC>(hyz);
+            }
+            const T hyx = lane > 0 ? sm.h[bc][1][ty + 1][xo - 1] : sm.hx1[bc][0][ty + 1];
+            const T hzx = lane > 0 ? sm.h[bc][2][ty + 1][xo - 1] : sm.hx1[bc][1][ty + 1];
+            T cur[3][VEC];
+            epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
+            T ex[VEC], ey[VEC], ez[VEC];
+            ldg_v<T, VEC>(ex, Ein + n);
+            ldg_v<T, VEC>(ey, Ein + g.N + n);
+            ldg_v<T, VEC>(ez, Ein + 2 * g.N + n);
+            epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, J, n, i0, j, k, use_cond, g, b, pl, st);
+            st_v<T, VEC>(Eout + n, ex);
+            st_v<T, VEC>(Eout + g.N + n, ey);
+            st_v<T, VEC>(Eout + 2 * g.N + n, ez);
+        }
+    }
 }
 
 // ---------------------------------------------------------------- staged kernels

@@ -47,8 +47,12 @@ class RoutinesMixin:
         try:
             fast = (callback is None and not save and type(source) in (PlaneWave, WavePacket)
                     and not self._force_explicit)
+            free = (source is None and callback is None and not save and not self._force_explicit
+                    and self._beam is None)
             if fast and Nt > 0:
                 self._emsolve_device(Nt, source)
+            elif free and Nt > 0:
+                self._emsolve_free(Nt)
             else:
                 for n in range(Nt):
                     if source is not None:
@@ -66,6 +70,22 @@ class RoutinesMixin:
             self._force_explicit = False
             if hfs is not None:
                 self._close_saves(hfs)
+
+    def _emsolve_free(self, Nt):
+        """emsolve without a source or callback: the first step through the host path
+        (ghost zeroing; explicit J while J is not sigma*E yet), the rest as one device
+        loop (CUDA graphs, the fused kernel when selected)."""
+        self._advance(self.nstep)
+        if Nt == 1:
+            return
+        if self._choose_mode() != nat.FIT_J_ELIDED:
+            for _ in range(Nt - 1):
+                self.one_step()
+            return
+        n0 = self.nstep
+        self._device_steps(n0, Nt - 1)
+        self.nstep = n0 + Nt - 1
+        self._after_device_run()
 
     def _emsolve_device(self, Nt, source):
         if source.is_first_update:
@@ -207,6 +227,8 @@ class RoutinesMixin:
             self._set_ghosts_to_0()
             self.step_0 = False
         self._sync_coeffs()
+        if self._kernels == "fused" and nsteps >= 256:
+            self.tune_fused()  # once per grid shape; leaves the fields unchanged
         self._ctx.call("fit_run", n0, nsteps)
         self._run_steps += nsteps
 

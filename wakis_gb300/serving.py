@@ -178,9 +178,12 @@ class ServedSolve:
         self.solver = self.wake = self.grid = self.beam = None
 
 
-def solve_alone(req, dtype=np.float32, device=0, dt=None):
-    """The request through the plain public API (SolverFIT3D.wakesolve), one at a time."""
+def solve_alone(req, dtype=np.float32, device=0, dt=None, kernels="auto"):
+    """The request through the plain public API (SolverFIT3D.wakesolve), one at a time.
+    kernels='direct' runs the two-pass kernels, whose per-cell code the pool shares (the
+    pooled result then equals this one bit for bit)."""
     grid, wake, solver = build(req, dtype, device, dt=dt)
+    solver.kernels = kernels
     solver.wakesolve(wakelength=req.wakelength, compute_plane="both")
     out = dict(s=wake.s, WP=wake.WP, WPx=wake.WPx, WPy=wake.WPy, f=wake.f, Z=wake.Z, Zx=wake.Zx, Zy=wake.Zy,
                Nt=solver.Nt, cells=req.cells)

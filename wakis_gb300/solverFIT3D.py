@@ -15,6 +15,7 @@ to E or J first brings J up to date, and the next step then reads J explicitly, 
 results are those of the reference's J.
 """
 
+import os
 import time
 
 import numpy as np
@@ -156,6 +157,8 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._ctx.call("fit_set_metrics", *[nat.dptr(a) for a in self._metric_arrays])
         self._coeff_dt = None
         self._sync_coeffs()
+        self._kernels = "direct"
+        self.kernels = os.environ.get("WAKIS_GB300_KERNELS", "auto")
 
         self.E._on_write = self._before_E_write
         self._J._on_write = self._before_J_write
@@ -165,6 +168,81 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self.update_logger(["solverInitializationTime"])
         if verbose:
             print(f"Total solver initialization time: {self.solverInitializationTime} s")
+
+    # ------------------------------------------------------------------ step kernels
+    _KERNELS = {"direct": 0, "staged": 1, "fused": 2}
+
+    @property
+    def kernels(self):
+        """Kernels of the device step loop (wakesolve, emsolve without Python sources):
+        'direct' (H and E pass kernels), 'staged' (persistent bulk-copy pass kernels) or
+        'fused' (one kernel per step that reads and writes each field value once; it
+        holds a second copy of E and H on the device and needs an even Nx).  'auto', the
+        default, is 'fused' where it applies and 'direct' elsewhere.  Single steps always
+        use the pass kernels.  The environment variable WAKIS_GB300_KERNELS sets the
+        default.  The fused step's tile shape is autotuned on the first long device loop
+        of each grid shape (tune_fused)."""
+        return self._kernels
+
+    @kernels.setter
+    def kernels(self, name):
+        key = str(name).lower()
+        self._kernels_auto = key == "auto"
+        if key == "auto":
+            key = "fused" if self.Nx % 2 == 0 else "direct"
+        if key not in self._KERNELS:
+            raise ValueError(f"kernels must be 'auto' or one of {sorted(self._KERNELS)}, got {name!r}")
+        self._ctx.call("fit_set_kernel_variant", self._KERNELS[key])
+        self._kernels = key
+        hit = SolverFIT3D._fused_shapes.get(self._grid_key())
+        if key == "fused" and hit is not None:
+            self._apply_tuned(*hit)
+
+    _fused_shapes = {}  # grid key -> ((vec, rows, zseg), times) chosen by tune_fused
+
+    def _grid_key(self):
+        return (self.Nx, self.Ny, self.Nz, np.dtype(self.dtype).name, bool(self.use_conductivity))
+
+    def tune_fused(self, reps=5, zsegs=(2, 4, 8, 16, 32, 64, 128), force=False):
+        """Autotuner of the fused step's tile shape for this grid: times every candidate
+        (cells per thread along x, rows per CTA, z ranges per tile column) with
+        fit_time_fused, which leaves E, H and J unchanged, keeps the fastest and
+        remembers it for grids of the same shape (later calls reuse it unless force).
+        Returns {(vec, rows, zseg): ms}."""
+        if self._kernels != "fused":
+            self.kernels = "fused"
+        key = self._grid_key()
+        if key in SolverFIT3D._fused_shapes and not force:
+            best, times = SolverFIT3D._fused_shapes[key]
+            self._apply_tuned(best, times)
+            return times
+        vecs = [v for v in ((4, 2) if self.dtype == np.float32 else (2,)) if self.Nx % v == 0]
+        if not vecs:
+            raise ValueError("the fused step needs Nx to be a multiple of 2")
+        self._sync_coeffs()
+        times = {}
+        ms = np.zeros(2)
+        for vec in vecs:
+            for rows in (4, 8):
+                for zseg in zsegs:
+                    if zseg > self.Nz:
+                        continue
+                    self._ctx.call("fit_set_fused_shape", vec, rows, zseg)
+                    self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
+                    times[(vec, rows, zseg)] = float(ms[0])
+        times["two-pass"] = float(ms[1])
+        best = min((t for t in times if t != "two-pass"), key=times.get)
+        SolverFIT3D._fused_shapes[key] = (best, times)
+        self._apply_tuned(best, times)
+        return times
+
+    def _apply_tuned(self, best, times):
+        """Sets the tuned fused shape; under kernels='auto' a grid on which the two-pass
+        step timed faster keeps the pass kernels."""
+        self._ctx.call("fit_set_fused_shape", *best)
+        if self._kernels_auto and times["two-pass"] < times[best]:
+            self._ctx.call("fit_set_kernel_variant", 0)
+            self._kernels = "direct"
 
     # ------------------------------------------------------------------ dt / coefficients
     @property
