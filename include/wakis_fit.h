@@ -294,6 +294,23 @@ FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
  * The serving layer's autotuner times the variants on the requests' own grids. */
 FIT_API int fit_pool_tune(FitPool *pool, int32_t vec, int32_t ctas_per_sm);
 
+/* ---------------------------------------------------------------- field monitor
+ * Running DFT of E at nf frequencies (FieldMonitor.update, wakis/field_monitors.py:59-101):
+ * acc[f][c][n] += E_c[n] * phase[f], accumulated in FP64 complex, in the reference's
+ * operation order.  acc (device) holds 3*nf*N complex128 values: component-major, then
+ * frequency, then the flat cell index.  phase: host (re, im) pairs.  single != 0 rounds
+ * each product to FP32 first, as numpy does for an FP32 field times a complex64 phase
+ * (the phase of an FP32 time step); FP64 fields ignore it. */
+/* One update from E (device, 3*N values of dtype), queued on stream (cudaStream_t; NULL =
+ * legacy default stream); returns after the update completes. */
+FIT_API int fit_monitor_update(const void *E, int32_t dtype, int64_t N, int32_t nf, const double *phase,
+                               void *acc, int32_t single, void *stream);
+/* Epilogue of the device step loop (fit_run; the wakesolve path with use_field_monitor):
+ * after each step n0 <= n < n0 + nsteps, acc += E^(n+1) * phases[n - n0][f]; phases holds
+ * nsteps*nf (re, im) pairs (copied to the device).  nf = 0 removes the epilogue. */
+FIT_API int fit_set_monitor(FitCtx *ctx, int32_t nf, const double *phases, int64_t n0, int64_t nsteps,
+                            void *acc, int32_t single);
+
 /* Library build information: sm architecture compiled for, and the kernel launch
  * counter (kernels issued since load), for bench accounting. */
 FIT_API int fit_version(char *buf, int64_t len);

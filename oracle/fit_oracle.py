@@ -467,9 +467,10 @@ class OracleWake:
         self.lambdas = None
 
 
-def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=None):
+def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=None, field_monitor=None):
     """Runs the time loop and returns the recorded Ez slab Ezs[n] = E_z(xx, yy, :) taken
-    after the beam update and before the step (wakis/routines.py:438-448).  Then calls
+    after the beam update and before the step (wakis/routines.py:438-448); a field
+    monitor is updated with E after each step (wakis/routines.py:450-451).  Then calls
     the post-processing.  Returns the recorded slabs (float64)."""
     if wakelength is None:
         wakelength = wake.wakelength
@@ -494,6 +495,8 @@ def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=
         beam.update(solver, n * solver.dt)
         slabs.append(np.array(ez[xx, yy, :], dtype=np.float64))
         solver.one_step()
+        if field_monitor is not None:
+            field_monitor.update(solver.E, solver.dt, solver.grid.shape)
     slabs = np.array(slabs)
     wake.t = t
     wake.zf = z.copy()
@@ -503,6 +506,37 @@ def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=
     wake.Nt = Nt
     postprocess(wake, slabs, compute_plane)
     return slabs
+
+
+class OracleFieldMonitor:
+    """Running DFT of E (wakis/field_monitors.py:14-116): after each update the
+    accumulators hold sum_n E^n * exp(-2j*pi*f*t_n), t_n = n*dt, complex128, shape
+    (n_freq, Nx, Ny, Nz); dt is fixed at the first update (field_monitors.py:76-88)."""
+
+    def __init__(self, frequencies):
+        self.frequencies = np.array(frequencies)
+        self.time_index = 0
+        self.dt = None
+        self.Ex_acc = self.Ey_acc = self.Ez_acc = None
+        self.shape = None
+
+    def update(self, E, dt, shape):
+        if self.dt is None:
+            self.dt = dt
+            self.shape = tuple(shape)
+            n = len(self.frequencies)
+            self.Ex_acc = np.zeros((n, *self.shape), dtype=np.complex128)
+            self.Ey_acc = np.zeros((n, *self.shape), dtype=np.complex128)
+            self.Ez_acc = np.zeros((n, *self.shape), dtype=np.complex128)
+        t = self.time_index * self.dt
+        N = int(np.prod(self.shape))
+        Ex, Ey, Ez = (comp_view(E, N, self.shape, d) for d in range(3))
+        for i, f in enumerate(self.frequencies):
+            phase = np.exp(-2j * np.pi * f * t)
+            self.Ex_acc[i] += Ex * phase
+            self.Ey_acc[i] += Ey * phase
+            self.Ez_acc[i] += Ez * phase
+        self.time_index += 1
 
 
 def wp_index_table(wake, nt_saved):

@@ -181,6 +181,10 @@ CASES = {
         bc_high=["periodic", "periodic", "pec"], cfln=0.5, random_init=41, Nt=20),
 }
 
+# wake runs with a FieldMonitor (running DFT of E after every step) attached
+CASES["monitor_f64"] = dict(CASES["cavity_f64"], monitor=[1.0e9, 3.0e9, 4.5e9])
+CASES["monitor_f32"] = dict(CASES["lossy_f32"], monitor=[2.0e9, 5.0e9])
+
 
 def axes(c):
     return _axes(c)

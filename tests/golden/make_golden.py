@@ -65,9 +65,18 @@ def run_wake(wakis, name, case, out):
     wake = wakis.WakeSolver(wakelength=case["wakelength"], save=False, verbose=0,
                             Ez_file=os.path.join(os.getcwd(), name + "_Ez.h5"), **w)
     solver = make_solver(wakis, case, grid, wake)
-    solver.wakesolve(wakelength=case["wakelength"], compute_plane=case["compute_plane"])
+    mon = None
+    kw = {}
+    if "monitor" in case:
+        from wakis.field_monitors import FieldMonitor
+        mon = FieldMonitor(case["monitor"])
+        kw = dict(use_field_monitor=True, field_monitor=mon)
+    solver.wakesolve(wakelength=case["wakelength"], compute_plane=case["compute_plane"], **kw)
     res = dict(Nt=solver.Nt, dt=np.float64(solver.dt), s=wake.s, WP=wake.WP, f=wake.f, Z=wake.Z,
                lambdas=wake.lambdas, E=solver.E.toarray(), H=solver.H.toarray(), J=solver.J.toarray())
+    if mon is not None:
+        comps = mon.get_components()
+        res.update(Ex_acc=comps["Ex"], Ey_acc=comps["Ey"], Ez_acc=comps["Ez"])
     if case["compute_plane"] != "longitudinal":
         res.update(WP_3d=wake.WP_3d, WPx=wake.WPx, WPy=wake.WPy, Zx=wake.Zx, Zy=wake.Zy)
     out[name] = res

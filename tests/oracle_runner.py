@@ -55,9 +55,12 @@ def run_oracle_case(name, case=None):
     s = oracle_solver(case)
     if kind == "wake":
         wake = O.OracleWake(wakelength=case["wakelength"], **case["wake"])
-        O.wakesolve(s, wake, case["wakelength"], case["compute_plane"])
+        mon = O.OracleFieldMonitor(case["monitor"]) if "monitor" in case else None
+        O.wakesolve(s, wake, case["wakelength"], case["compute_plane"], field_monitor=mon)
         res = dict(Nt=s.Nt, dt=np.float64(s.dt), s=wake.s, WP=wake.WP, f=wake.f, Z=wake.Z,
                    lambdas=wake.lambdas, E=s.E.copy(), H=s.H.copy(), J=s.J.copy())
+        if mon is not None:
+            res.update(Ex_acc=mon.Ex_acc, Ey_acc=mon.Ey_acc, Ez_acc=mon.Ez_acc)
         if case["compute_plane"] != "longitudinal":
             res.update(WP_3d=wake.WP_3d, WPx=wake.WPx, WPy=wake.WPy, Zx=wake.Zx, Zy=wake.Zy)
         return res

@@ -52,9 +52,14 @@ def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None, dt=No
                              **case["wake"])
         s = make_solver(wg, case, grid, wake, dtype, dt)
         s.logger.wakeSolver["results_folder"] = str(tmpdir)
-        s.wakesolve(wakelength=case["wakelength"], compute_plane=case["compute_plane"])
+        mon = wg.FieldMonitor(case["monitor"]) if "monitor" in case else None
+        cb = (lambda sv, t: None) if userloop_wake else None
+        s.wakesolve(wakelength=case["wakelength"], compute_plane=case["compute_plane"], callback=cb,
+                    use_field_monitor=mon is not None, field_monitor=mon)
         res = dict(Nt=s.Nt, dt=np.float64(s.dt), s=wake.s, WP=wake.WP, f=wake.f, Z=wake.Z, lambdas=wake.lambdas,
                    E=s.E.numpy(), H=s.H.numpy(), J=s.J.numpy())
+        if mon is not None:
+            res.update({k + "_acc": v.cpu().numpy() for k, v in mon.get_components().items()})
         if case["compute_plane"] != "longitudinal":
             res.update(WP_3d=wake.WP_3d, WPx=wake.WPx, WPy=wake.WPy, Zx=wake.Zx, Zy=wake.Zy)
         return res

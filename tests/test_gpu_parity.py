@@ -47,7 +47,7 @@ def _compare(name, got, ref, what):
             assert got[k] == v, f"{what} {name}: dt {got[k]} != {v}"
         elif k in ("s", "f"):
             np.testing.assert_array_equal(got[k], v, err_msg=f"{what} {name}: {k}")
-        elif k in ("E", "H", "J", "probes", "Ey"):
+        elif k in ("E", "H", "J", "probes", "Ey") or k.endswith("_acc"):
             e = _err(got[k], v)
             assert e <= FIELD_TOL[dt], f"{what} {name}: {k} rel L2 {e:.3e}"
         elif k in ("WPx", "WPy"):

@@ -10,6 +10,7 @@ __version__ = "0.1.0"
 
 from . import materials, sources  # noqa: F401
 from .field import Field  # noqa: F401
+from .field_monitors import FieldMonitor  # noqa: F401
 from .gridFIT3D import GridFIT3D  # noqa: F401
 from .logger import Logger  # noqa: F401
 from .solverFIT3D import SolverFIT3D  # noqa: F401

@@ -88,6 +88,8 @@ struct FitCtx {
     void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
     int fused_vec = 4, fused_rows = 8, fused_zseg = 1;  // tile shape of the fused step
     bool graph_fused = false;  // the cached graph holds fused steps
+    MonitorArgs mon{};          // field monitor epilogue of device-loop steps (nf = 0: off)
+    double2* d_mon_phases = nullptr;
     std::atomic<bool> in_pool{false};  // submitted to a FitPool and not yet reported done
     std::string err;
 };
@@ -209,7 +211,7 @@ void invalidate(FitCtx* c) {
 }
 
 int launches_per_step(const FitCtx* c) {
-    int n = 3;
+    int n = 3 + (c->mon.nf > 0);
     for (int a = 0; a < 3; ++a) n += (c->abc_axes >> a) & 1;
     return n;
 }
@@ -283,6 +285,18 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
     count(c);
 }
 
+// the field-monitor epilogue of a step whose new E is in E (device loop: step number
+// from the counter; host step: n)
+template <typename T>
+void launch_monitor(FitCtx* c, const T* E, bool device_step, long long n) {
+    if (c->mon.nf <= 0) return;
+    const long long n3 = 3 * c->g.N;
+    const unsigned grid = (unsigned)std::min<long long>(grid1d(n3, 256), 8LL * c->nsm);
+    k_monitor<T><<<grid, 256, 0, c->own>>>(E, c->g.N, c->mon, device_step ? c->d_step : nullptr,
+                                          device_step ? -1 : n);
+    count(c);
+}
+
 template <typename T>
 void launch_step_t(FitCtx* c, long long n, int mode, bool device_step) {
     StepArgs st{};
@@ -322,6 +336,7 @@ void launch_step_t(FitCtx* c, long long n, int mode, bool device_step) {
             count(c);
         }
     }
+    launch_monitor<T>(c, static_cast<const T*>(c->E), device_step, n);
 }
 
 void launch_step(FitCtx* c, long long n, int mode, bool device_step) {
@@ -396,12 +411,14 @@ void launch_fused_step(FitCtx* c, int mode, bool forward, const StepArgs& st, lo
                                                    n, dev ? c->d_step : nullptr);
         count(c);
         launch_fused(c, mode, st, forward, c->beam);
+        launch_monitor<double>(c, static_cast<const double*>(forward ? c->E2 : c->E), dev, n);
     } else {
         k_prologue<float><<<1, 512, 0, c->own>>>(static_cast<float*>(forward ? c->E : c->E2),
                                                  static_cast<float*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
                                                  n, dev ? c->d_step : nullptr);
         count(c);
         launch_fused(c, mode, st, forward, c->beam);
+        launch_monitor<float>(c, static_cast<const float*>(forward ? c->E2 : c->E), dev, n);
     }
 }
 
@@ -521,7 +538,7 @@ int fit_ctx_destroy(FitCtx* c) {
         dfree(c->tL_T[a], c->own);
         dfree(c->L_T[a], c->own);
     }
-    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg, c->E2, c->H2}) dfree(p, c->own);
+    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg, c->E2, c->H2, (void*)c->d_mon_phases}) dfree(p, c->own);
     for (void* p : {(void*)c->d_beam_z, (void*)c->d_beam_dtieps, (void*)c->d_vt_table, (void*)c->d_prof,
                     (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
                     (void*)c->d_em, (void*)c->d_ek0, (void*)c->d_ecnt, (void*)c->d_dz, (void*)c->d_acc,
@@ -928,7 +945,7 @@ int fit_run(FitCtx* c, int64_t n0, int64_t nsteps) {
         }
         while (nsteps - done >= chunk) {
             CK(cudaGraphLaunch(c->graph, c->own));
-            g_launches += chunk * 2;
+            g_launches += chunk * (2 + (c->mon.nf > 0));
             done += chunk;
         }
         for (; done < nsteps; done += 2) {
@@ -1154,6 +1171,30 @@ int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg) {
     return FIT_OK;
 }
 
+int fit_set_monitor(FitCtx* c, int32_t nf, const double* phases, int64_t n0, int64_t nsteps, void* acc,
+                    int32_t single) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    invalidate(c);
+    if (nf <= 0) {
+        c->mon = MonitorArgs{};
+        return FIT_OK;
+    }
+    if (!phases || !acc || nsteps <= 0 || n0 < 0) return fail(c, FIT_ERR_ARG, "bad field monitor arguments");
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = upload(c, &c->d_mon_phases, phases, (size_t)nsteps * nf * sizeof(double2));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->own));
+    c->mon.nf = nf;
+    c->mon.single = single != 0;
+    c->mon.phases = c->d_mon_phases;
+    c->mon.n0 = n0;
+    c->mon.nsteps = nsteps;
+    c->mon.acc = static_cast<double2*>(acc);
+    return leave(c);
+}
+
 int fit_time_fused(FitCtx* c, int32_t reps, double* ms_out) {
     int rc = check_ready(c);
     if (rc) return rc;
@@ -1291,3 +1332,35 @@ extern "C" int fit_dft_noalloc(const double* x, int32_t nsig, int64_t len, int64
 
 // serving pool (continuous batching of FP32 wake solves)
 #include "fit_pool.cuh"
+
+// ---------------------------------------------------------------------------------------
+// Host-driven field monitor update (FieldMonitor.update): acc += E * phase, stream-ordered.
+extern "C" int fit_monitor_update(const void* E, int32_t dtype, int64_t N, int32_t nf, const double* phase, void* acc,
+                                  int32_t single, void* stream) {
+    if (!E || !phase || !acc || N <= 0 || nf <= 0 || (dtype != FIT_F32 && dtype != FIT_F64))
+        return fail(nullptr, FIT_ERR_ARG, "bad fit_monitor_update arguments");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) keep_freed_blocks(dev);
+    double2* dph = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync(&dph, nf * sizeof(double2), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dph, phase, nf * sizeof(double2), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "fit_monitor_update: %s", cudaGetErrorString(e));
+    MonitorArgs m{};
+    m.nf = nf;
+    m.single = single != 0;
+    m.phases = dph;
+    m.acc = static_cast<double2*>(acc);
+    const unsigned grid = (unsigned)std::min<long long>(grid1d(3 * N, 256), 4096);
+    if (dtype == FIT_F64)
+        k_monitor<double><<<grid, 256, 0, st>>>(static_cast<const double*>(E), N, m, nullptr, -1);
+    else
+        k_monitor<float><<<grid, 256, 0, st>>>(static_cast<const float*>(E), N, m, nullptr, -1);
+    g_launches++;
+    e = cudaGetLastError();
+    cudaFreeAsync(dph, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host phase array is read before returning
+    if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "fit_monitor_update: %s", cudaGetErrorString(e));
+    return FIT_OK;
+}

@@ -1282,6 +1282,53 @@ __global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneAr
     }
 }
 
+// Field monitor (FieldMonitor.update, wakis/field_monitors.py:59-101): running DFT of E
+// at nf frequencies, acc[f][c][n] += E_c[n] * phase[f], accumulated in FP64 (complex128),
+// with the operation order of the reference's complex product of a real field value by
+// the phase: re += e*pr, im += e*pi (no fused multiply-add).  With single set the
+// products are rounded to FP32 first: numpy evaluates an FP32 field times a phase taken
+// from an FP32 time in complex64.  The phase row of a device-loop step is
+// phases[(*d_step - 1) - n0] (the prologue advanced the counter before the passes).
+struct MonitorArgs {
+    int nf;
+    int single;             // products in FP32 (FP32 field, complex64 phases)
+    const double2* phases;  // steps x nf, or the nf phases of one host-driven update
+    long long n0, nsteps;   // device loop: steps n0 <= n < n0 + nsteps are monitored
+    double2* acc;           // [3][nf][N]
+};
+
+template <typename T>
+__global__ void k_monitor(const T* __restrict__ E, long long N, MonitorArgs m, const long long* d_step, long long n_arg) {
+    const double2* ph = m.phases;
+    if (d_step || n_arg >= 0) {
+        const long long n = d_step ? *d_step - 1 : n_arg;
+        if (n < m.n0 || n >= m.n0 + m.nsteps) return;
+        ph += (n - m.n0) * m.nf;
+    }
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < 3 * N;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long c = idx / N, n = idx - c * N;
+        const T ev = E[idx];
+        const double e = (double)ev;
+        for (int f = 0; f < m.nf; ++f) {
+            const double2 p = ph[f];
+            double2* a = m.acc + (c * m.nf + f) * N + n;
+            double2 v = *a;
+            double px, py;
+            if (sizeof(T) == 4 && m.single) {
+                px = (double)__fmul_rn((float)ev, (float)p.x);
+                py = (double)__fmul_rn((float)ev, (float)p.y);
+            } else {
+                px = __dmul_rn(e, p.x);
+                py = __dmul_rn(e, p.y);
+            }
+            v.x = __dadd_rn(v.x, px);
+            v.y = __dadd_rn(v.y, py);
+            *a = v;
+        }
+    }
+}
+
 // J = sigma*E (field dtype) and the beam line
 template <typename T>
 __global__ void k_materialize_J(const T* __restrict__ E, T* __restrict__ J, const double* __restrict__ sigma,

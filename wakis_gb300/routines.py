@@ -17,6 +17,7 @@ import time
 import numpy as np
 
 from . import _native as nat
+from .field_monitors import FieldMonitor
 from .sources import Beam, PlaneWave, WavePacket
 
 
@@ -146,11 +147,22 @@ class RoutinesMixin:
         if self.verbose:
             print("Running electromagnetic time-domain simulation...")
         t0 = time.time()
-        fast = callback is None and not (use_field_monitor and field_monitor is not None)
+        monitor = field_monitor if (use_field_monitor and field_monitor is not None) else None
+        fast = callback is None and (monitor is None or isinstance(monitor, FieldMonitor))
         if fast and Nt > 0:
             vt = self._wake_device_setup(beam, Nt)
             first = self._wake_first_step(beam)
-            self._device_steps(first, Nt - first)
+            if monitor is not None and first > 0:
+                monitor.update(self.E, self.dt)
+            if monitor is not None and Nt > first:
+                self._attach_monitor(monitor, first, Nt - first)
+            try:
+                self._device_steps(first, Nt - first)
+            finally:
+                if monitor is not None:
+                    self._ctx.call("fit_set_monitor", 0, None, 0, 0, None, 0)
+            if monitor is not None:
+                monitor.time_index += Nt - first
             self._wake_device_done(vt, Nt)
         else:
             for n in range(Nt):
@@ -220,6 +232,15 @@ class RoutinesMixin:
         self._after_device_run()
 
     # ------------------------------------------------------------------ helpers
+    def _attach_monitor(self, monitor, n0, nsteps):
+        """FieldMonitor as the epilogue of device-loop steps n0 .. n0+nsteps-1: the phase
+        table continues the monitor's own time index."""
+        if monitor.dt is None:
+            monitor._init(self.E, self.dt)
+        ph, single = monitor._pairs(monitor.phases(monitor.time_index, nsteps), self.dtype)
+        self._ctx.call("fit_set_monitor", len(monitor.frequencies), nat.dptr(ph), int(n0), int(nsteps),
+                       nat.C.c_void_p(monitor._acc.data_ptr()), single)
+
     def _device_steps(self, n0, nsteps):
         if nsteps <= 0:
             return
