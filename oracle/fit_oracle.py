@@ -440,6 +440,89 @@ class OracleWavePacket:
 # --------------------------------------------------------------------------------------
 # drivers: wakis/routines.py:17-229 (emsolve) and 231-485 (wakesolve)
 # --------------------------------------------------------------------------------------
+class _OraclePointSource:
+    """Hard source on an index region of one field component (wakis/sources.py:458-762:
+    the common part of Dipole and Pulse).  'Ex'-style field names carry the component;
+    regions default to the grid centre."""
+
+    def __init__(self, field, component, xs, ys, zs, amplitude):
+        self.xs, self.ys, self.zs = xs, ys, zs
+        self.field, self.component, self.amplitude = field, component, amplitude
+        if len(field) == 2:
+            self.field, self.component = field[0], field[1]
+        self.is_first_update = True
+
+    def _centre(self, solver):
+        if self.xs is None:
+            self.xs = int(solver.Nx / 2)
+        if self.ys is None:
+            self.ys = int(solver.Ny / 2)
+        if self.zs is None:
+            self.zs = int(solver.Nz / 2)
+
+    def _write(self, solver, value):
+        arr = {"E": solver.E, "H": solver.H, "J": solver.J}.get(self.field)
+        if arr is None:
+            return
+        solver.comp(arr, "xyz".index(self.component))[self.xs, self.ys, self.zs] = value
+
+
+class OracleDipole(_OraclePointSource):
+    """amplitude*sin(w t + phase), f = nodes / ((zmax - zmin)/c) unless given
+    (wakis/sources.py:458-565)."""
+
+    def __init__(self, field="E", component="z", xs=None, ys=None, zs=None, nodes=10, f=None, amplitude=1.0,
+                 phase=0):
+        super().__init__(field, component, xs, ys, zs, amplitude)
+        self.nodes, self.f, self.phase = nodes, f, phase
+
+    def update(self, solver, t):
+        if self.is_first_update:
+            self._centre(solver)
+            if self.f is None:
+                T = (solver.z.max() - solver.z.min()) / c_light
+                self.f = self.nodes / T
+            self.w = 2 * np.pi * self.f
+            self.is_first_update = False
+        self._write(solver, self.amplitude * np.sin(self.w * t + self.phase))
+
+
+class OraclePulse(_OraclePointSource):
+    """Harris / Gaussian / rectangular pulse in t*c - delay of width L (default 50 dt)
+    (wakis/sources.py:567-762)."""
+
+    def __init__(self, field="E", component="z", xs=None, ys=None, zs=None, shape="Harris", L=None, amplitude=1.0,
+                 delay=0.0):
+        super().__init__(field, component, xs, ys, zs, amplitude)
+        self.shape, self.L, self.delay = shape, L, delay
+        self.tprofile = {"harris": self.harris, "gaussian": self.gaussian,
+                         "rectangular": self.rectangular}[shape.lower()]
+
+    def _harris_value(self, x):
+        return (10 - 15 * np.cos(2 * np.pi / self.L * x) + 6 * np.cos(4 * np.pi / self.L * x)
+                - np.cos(6 * np.pi / self.L * x)) / 32
+
+    def harris(self, t):
+        x = t * c_light - self.delay
+        return self._harris_value(x) if x < self.L else 0.0
+
+    def gaussian(self, t):
+        x = t * c_light - self.delay
+        return np.exp(-((x - 5 * (self.L / 10)) ** 2) / (2 * (self.L / 10) ** 2))
+
+    def rectangular(self, t):
+        x = t * c_light - self.delay
+        return 1.0 if (x < self.L and x > 0.0) else 0.0
+
+    def update(self, solver, t):
+        if self.is_first_update:
+            self._centre(solver)
+            if self.L is None:
+                self.L = 50 * solver.dt
+            self.is_first_update = False
+        self._write(solver, self.amplitude * self.tprofile(t))
+
+
 def emsolve(solver, Nt, source=None, callback=None):
     for n in range(Nt):
         if source is not None:

@@ -181,6 +181,38 @@ CASES = {
         bc_high=["periodic", "periodic", "pec"], cfln=0.5, random_init=41, Nt=20),
 }
 
+# point / region hard sources driven through the Field API every step (emsolve host loop)
+_box = dict(xmin=-1.0, xmax=1.0, ymin=-1.0, ymax=1.0, zmin=-1.0, zmax=1.0)
+CASES["dipole_f64"] = dict(
+    kind="emsolve", dtype="float64", grid=dict(_box, Nx=12, Ny=12, Nz=16),
+    solids=[("diel", "block", {"lo": (-0.6, -0.6, 0.2), "hi": (0.5, 0.4, 0.8)}, [3.0, 1.0])], bg=[1.0, 1.0],
+    bc_low=["pec", "pec", "pec"], bc_high=["pec", "pec", "pec"], cfln=0.5, Nt=120,
+    source=dict(type="Dipole", field="E", component="z", nodes=3, amplitude=2.0, phase=0.4))
+CASES["pulse_harris_f32"] = dict(
+    kind="emsolve", dtype="float32", grid=dict(_box, Nx=14, Ny=12, Nz=18),
+    solids=[("lossy", "block", {"lo": (-1.0, -1.0, 0.3), "hi": (1.0, 1.0, 0.7)}, [1.0, 1.0, 20.0])],
+    bg=[1.0, 1.0], bc_low=["pec", "pec", "pml"], bc_high=["pec", "pec", "pml"], n_pml=3, cfln=0.5, Nt=140,
+    source=dict(type="Pulse", field="Hy", shape="Harris", xs=(4, 9), ys=6, zs=5, L=0.8, amplitude=1.5))
+CASES["pulse_gauss_j_f64"] = dict(
+    kind="emsolve", dtype="float64", grid=dict(_box, Nx=10, Ny=12, Nz=14),
+    solids=[("lossy", "block", {"lo": (-0.4, -0.4, -0.4), "hi": (0.4, 0.4, 0.4)}, [2.0, 1.0, 5.0])],
+    bg=[1.0, 1.0], bc_low=["pec", "pml", "pec"], bc_high=["pec", "pml", "pec"], n_pml=3, cfln=0.5, Nt=100,
+    source=dict(type="Pulse", field="J", component="x", shape="Gaussian", xs=5, ys=6, zs=7, L=1.0, amplitude=1e3))
+CASES["pulse_rect_f64"] = dict(
+    kind="emsolve", dtype="float64", grid=dict(_box, Nx=12, Ny=10, Nz=12),
+    solids=[], bg=[1.0, 1.0], bc_low=["pec", "pec", "pec"], bc_high=["pec", "pec", "pec"], cfln=0.5, Nt=90,
+    source=dict(type="Pulse", field="Ex", shape="Rectangular", xs=(3, 8), ys=(2, 5), zs=6, L=0.6,
+                delay=0.05, amplitude=0.7))
+
+
+def point_source(module, sc):
+    """A Dipole or Pulse of `module.sources` from a case's source description (index
+    spans given as (start, stop) become slices)."""
+    kw = {k: (slice(*v) if k in ("xs", "ys", "zs") and isinstance(v, tuple) else v)
+          for k, v in sc.items() if k != "type"}
+    return getattr(module.sources, sc["type"])(**kw)
+
+
 # wake runs with a FieldMonitor (running DFT of E after every step) attached
 CASES["monitor_f64"] = dict(CASES["cavity_f64"], monitor=[1.0e9, 3.0e9, 4.5e9])
 CASES["monitor_f32"] = dict(CASES["lossy_f32"], monitor=[2.0e9, 5.0e9])

@@ -97,6 +97,8 @@ def run_emsolve(wakis, name, case, out):
     elif sc is not None and sc["type"] == "WavePacket":
         src = wakis.sources.WavePacket(zs=sc["zs"], sigmaz=sc["sigmaz"], sigmaxy=sc["sigmaxy"],
                                        wavelength=sc["wavelength"], amplitude=sc["amplitude"])
+    elif sc is not None:
+        src = C.point_source(wakis, sc)
     if "random_init" in case:
         E0, H0 = C.random_fields(solver.N, case["random_init"], solver.E.toarray().dtype)
         solver.E.fromarray(E0)

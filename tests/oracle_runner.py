@@ -36,6 +36,13 @@ def oracle_solver(case):
                           cfln=case.get("cfln", 0.5), dtype=dtype, n_pml=case.get("n_pml", 10))
 
 
+class _ORACLE_SOURCES:
+    """The oracle's point sources under the names the case descriptions use."""
+    class sources:
+        Dipole = O.OracleDipole
+        Pulse = O.OraclePulse
+
+
 def run_oracle_case(name, case=None):
     case = case or C.CASES[name]
     kind = case["kind"]
@@ -82,6 +89,8 @@ def run_oracle_case(name, case=None):
     elif sc is not None and sc["type"] == "WavePacket":
         src = O.OracleWavePacket(zs=sc["zs"], sigmaz=sc["sigmaz"], sigmaxy=sc["sigmaxy"],
                                  wavelength=sc["wavelength"], amplitude=sc["amplitude"])
+    elif sc is not None:
+        src = C.point_source(_ORACLE_SOURCES, sc)
     if "random_init" in case:
         E0, H0 = C.random_fields(s.N, case["random_init"], s.E.dtype)
         s.E[:] = E0

@@ -81,6 +81,8 @@ def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None, dt=No
     elif sc is not None and sc["type"] == "WavePacket":
         src = wg.sources.WavePacket(zs=sc["zs"], sigmaz=sc["sigmaz"], sigmaxy=sc["sigmaxy"],
                                     wavelength=sc["wavelength"], amplitude=sc["amplitude"])
+    elif sc is not None:
+        src = C.point_source(wg, sc)
     if "random_init" in case:
         E0, H0 = C.random_fields(s.N, case["random_init"], np.dtype(s.dtype))
         s.E.fromarray(E0)

@@ -183,3 +183,101 @@ class WavePacket:
 
     def plot(self, t, zmin=0):
         raise NotImplementedError("plotting is not provided")
+
+
+class _PointSource:
+    """Hard source on an index region of one field component: the part Dipole and Pulse
+    share (wakis/sources.py:458-762).  ``field`` is 'E', 'H' or 'J', or 'Ex'-style with the
+    component; xs, ys, zs are indices or slices and default to the grid centre.  The
+    value is written through the solver's Field API every update, so the E / J
+    bookkeeping of the solver (explicit J after a J write) applies as for any user write."""
+
+    def __init__(self, field, component, xs, ys, zs, amplitude):
+        self.xs, self.ys, self.zs = xs, ys, zs
+        self.field = field
+        self.component = component
+        self.amplitude = amplitude
+        if len(field) == 2:
+            self.component = field[1]
+            self.field = field[0]
+        self.is_first_update = True
+
+    def _centre(self, solver):
+        if self.xs is None:
+            self.xs = int(solver.Nx / 2)
+        if self.ys is None:
+            self.ys = int(solver.Ny / 2)
+        if self.zs is None:
+            self.zs = int(solver.Nz / 2)
+
+    def _write(self, solver, value):
+        if self.field in ("E", "H", "J"):
+            getattr(solver, self.field)[self.xs, self.ys, self.zs, self.component] = value
+        else:
+            print(f'Field "{self.field}" not valid, should be "E", "H" or "J"]')
+
+
+class Dipole(_PointSource):
+    """Sinusoidal excitation amplitude*sin(w t + phase) (wakis/sources.py:458-565); the
+    frequency is nodes / ((z.max - z.min)/c) unless f is given."""
+
+    def __init__(self, field="E", component="z", xs=None, ys=None, zs=None, nodes=10, f=None, amplitude=1.0,
+                 phase=0):
+        super().__init__(field, component, xs, ys, zs, amplitude)
+        self.nodes = nodes
+        self.f = f
+        self.phase = phase
+
+    def update(self, solver, t):
+        if self.is_first_update:
+            self._centre(solver)
+            if self.f is None:
+                T = (solver.z.max() - solver.z.min()) / c_light
+                self.f = self.nodes / T
+            self.w = 2 * np.pi * self.f
+            self.is_first_update = False
+        self._write(solver, self.amplitude * np.sin(self.w * t + self.phase))
+
+
+class Pulse(_PointSource):
+    """Pulse of width L (default 50 dt) in x = t*c - delay (wakis/sources.py:567-762):
+    'Harris' (four-term cosine window on 0 <= x < L), 'Gaussian' (sigma L/10 centred at
+    L/2) or 'Rectangular' (1 on 0 < x < L)."""
+
+    def __init__(self, field="E", component="z", xs=None, ys=None, zs=None, shape="Harris", L=None, amplitude=1.0,
+                 delay=0.0):
+        super().__init__(field, component, xs, ys, zs, amplitude)
+        self.shape = shape
+        self.L = L
+        self.delay = delay
+        profiles = {"harris": self.harris_pulse, "gaussian": self.gaussian_pulse,
+                    "rectangular": self.rectangular_pulse}
+        self.tprofile = profiles.get(shape.lower())
+        if self.tprofile is None:
+            print('** shape does not, match available types: "Harris", "Gaussian", "Rectangular"')
+
+    def _harris(self, x):
+        return (10 - 15 * np.cos(2 * np.pi / self.L * x) + 6 * np.cos(4 * np.pi / self.L * x)
+                - np.cos(6 * np.pi / self.L * x)) / 32
+
+    def harris_pulse(self, t):
+        x = t * c_light - self.delay
+        if np.ndim(x) > 0:  # time arrays: the window without the cut at L
+            return self._harris(x)
+        return self._harris(x) if x < self.L else 0.0
+
+    def gaussian_pulse(self, t):
+        x = t * c_light - self.delay
+        return np.exp(-((x - 5 * (self.L / 10)) ** 2) / (2 * (self.L / 10) ** 2))
+
+    def rectangular_pulse(self, t):
+        x = t * c_light - self.delay
+        return 1.0 if (x < self.L and x > 0.0) else 0.0
+
+    def update(self, solver, t):
+        if self.is_first_update:
+            self._centre(solver)
+            if self.L is None:
+                self.L = 50 * solver.dt
+            self.is_first_update = False
+        self._write(solver, self.amplitude * self.tprofile(t))
