@@ -311,6 +311,13 @@ FIT_API int fit_monitor_update(const void *E, int32_t dtype, int64_t N, int32_t 
 FIT_API int fit_set_monitor(FitCtx *ctx, int32_t nf, const double *phases, int64_t n0, int64_t nsteps,
                             void *acc, int32_t single);
 
+/* Ez line history (the reference's Ez.h5 dump, wakis/routines.py:379-446): at every step
+ * n0 <= n < n0 + nsteps, before the step (with the wake taps), E_z(lx[l], ly[l], k) of the
+ * nlines (<= 9) lines for all k is written to hist[n - n0][l][k] (device, field dtype,
+ * nsteps*nlines*Nz values).  nlines = 0 stops recording. */
+FIT_API int fit_set_ez_record(FitCtx *ctx, void *hist, int32_t nlines, const int32_t *lx, const int32_t *ly,
+                              int64_t n0, int64_t nsteps);
+
 /* Library build information: sm architecture compiled for, and the kernel launch
  * counter (kernels issued since load), for bench accounting. */
 FIT_API int fit_version(char *buf, int64_t len);

@@ -87,6 +87,7 @@ _SIGS = {
     "fit_set_fused_shape": (_P, C.c_int32, C.c_int32, C.c_int32),
     "fit_monitor_update": (_P, C.c_int32, C.c_int64, C.c_int32, _D, _P, C.c_int32, _P),
     "fit_set_monitor": (_P, C.c_int32, _D, C.c_int64, C.c_int64, _P, C.c_int32),
+    "fit_set_ez_record": (_P, _P, C.c_int32, _I32, _I32, C.c_int64, C.c_int64),
     "fit_pool_create": (C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)),
     "fit_pool_destroy": (_P,),
     "fit_pool_last_error": (_P, C.c_char_p, C.c_int64),

@@ -88,6 +88,7 @@ struct FitCtx {
     void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
     int fused_vec = 4, fused_rows = 8, fused_zseg = 1;  // tile shape of the fused step
     bool graph_fused = false;  // the cached graph holds fused steps
+    RecordArgs rec{};           // Ez line history of recorded steps (nlines = 0: off)
     MonitorArgs mon{};          // field monitor epilogue of device-loop steps (nf = 0: off)
     double2* d_mon_phases = nullptr;
     std::atomic<bool> in_pool{false};  // submitted to a FitPool and not yet reported done
@@ -308,10 +309,10 @@ void launch_step_t(FitCtx* c, long long n, int mode, bool device_step) {
         st.n = n;
         st.vt = c->beam_vt;
     }
-    const bool need_pro = device_step || c->plane.active || c->tap.nlines > 0;
+    const bool need_pro = device_step || c->plane.active || c->tap.nlines > 0 || c->rec.nlines > 0;
     if (need_pro) {
         k_prologue<T><<<1, 512, 0, c->own>>>(static_cast<T*>(c->E), static_cast<T*>(c->H), c->g, c->plane, c->tap,
-                                             n, device_step ? c->d_step : nullptr);
+                                             n, device_step ? c->d_step : nullptr, c->rec);
         count(c);
     }
     const int vec = pick_vec(c);
@@ -408,14 +409,14 @@ void launch_fused_step(FitCtx* c, int mode, bool forward, const StepArgs& st, lo
     if (c->dtype == FIT_F64) {
         k_prologue<double><<<1, 512, 0, c->own>>>(static_cast<double*>(forward ? c->E : c->E2),
                                                    static_cast<double*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
-                                                   n, dev ? c->d_step : nullptr);
+                                                   n, dev ? c->d_step : nullptr, c->rec);
         count(c);
         launch_fused(c, mode, st, forward, c->beam);
         launch_monitor<double>(c, static_cast<const double*>(forward ? c->E2 : c->E), dev, n);
     } else {
         k_prologue<float><<<1, 512, 0, c->own>>>(static_cast<float*>(forward ? c->E : c->E2),
                                                  static_cast<float*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
-                                                 n, dev ? c->d_step : nullptr);
+                                                 n, dev ? c->d_step : nullptr, c->rec);
         count(c);
         launch_fused(c, mode, st, forward, c->beam);
         launch_monitor<float>(c, static_cast<const float*>(forward ? c->E2 : c->E), dev, n);
@@ -1193,6 +1194,30 @@ int fit_set_monitor(FitCtx* c, int32_t nf, const double* phases, int64_t n0, int
     c->mon.nsteps = nsteps;
     c->mon.acc = static_cast<double2*>(acc);
     return leave(c);
+}
+
+int fit_set_ez_record(FitCtx* c, void* hist, int32_t nlines, const int32_t* lx, const int32_t* ly, int64_t n0,
+                      int64_t nsteps) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    invalidate(c);
+    if (nlines <= 0) {
+        c->rec = RecordArgs{};
+        return FIT_OK;
+    }
+    if (nlines > 9 || !hist || !lx || !ly || n0 < 0 || nsteps <= 0) return fail(c, FIT_ERR_ARG, "bad Ez record arguments");
+    RecordArgs r{};
+    for (int l = 0; l < nlines; ++l) {
+        if (lx[l] < 0 || lx[l] >= c->g.nx || ly[l] < 0 || ly[l] >= c->g.ny)
+            return fail(c, FIT_ERR_ARG, "Ez record line %d outside the grid", l);
+        r.base[l] = (long long)lx[l] + c->g.sy * ly[l];
+    }
+    r.hist = hist;
+    r.nlines = nlines;
+    r.n0 = n0;
+    r.nsteps = nsteps;
+    c->rec = r;
+    return FIT_OK;
 }
 
 int fit_time_fused(FitCtx* c, int32_t reps, double* ms_out) {

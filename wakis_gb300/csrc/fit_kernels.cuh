@@ -1258,9 +1258,19 @@ __device__ __forceinline__ void wake_taps(const T* __restrict__ E, const Geom& g
     }
 }
 
+// Ez line history (the reference's Ez.h5 dump, wakis/routines.py:438-446): E_z of each
+// recorded line over all z, taken with the wake taps (after the source update, before
+// the step), stored hist[n - n0][line][k] in the field dtype.
+struct RecordArgs {
+    void* hist;
+    int nlines;
+    long long base[9];  // flat index of E_z(lx, ly, 0) per line
+    long long n0, nsteps;
+};
+
 template <typename T>
 __global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneArgs pl, TapArgs tp,
-                           long long n_arg, long long* d_step) {
+                           long long n_arg, long long* d_step, RecordArgs rec) {
     const long long n = d_step ? *d_step : n_arg;
     // plane source
     if (pl.active && n >= 0 && n < pl.len) {
@@ -1273,6 +1283,14 @@ __global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneAr
             if (pl.stash) pl.stash[t] = (double)E[c];
             H[g.N + c] = (T)__dmul_rn(__dmul_rn(c1, pv), gt);
             E[c] = (T)__dmul_rn(__dmul_rn(c2, pv), gt);
+        }
+    }
+    if (rec.nlines > 0 && n >= rec.n0 && n < rec.n0 + rec.nsteps) {
+        T* h = static_cast<T*>(rec.hist) + (n - rec.n0) * rec.nlines * (long long)g.nz;
+        const T* Ez = E + 2 * g.N;
+        for (int t = threadIdx.x; t < rec.nlines * g.nz; t += blockDim.x) {
+            const int l = t / g.nz, k = t - l * g.nz;
+            h[t] = Ez[rec.base[l] + g.sz * k];
         }
     }
     wake_taps<T>(E, g, tp, n);

@@ -15,6 +15,7 @@ tables; other sources, callbacks and saving run the loop step by step.
 import time
 
 import numpy as np
+import torch
 
 from . import _native as nat
 from .field_monitors import FieldMonitor
@@ -128,7 +129,12 @@ class RoutinesMixin:
     # ------------------------------------------------------------------ wakesolve
     def wakesolve(self, wakelength=None, wake=None, callback=None, compute_plane="both", plot=False, plot_func=None,
                   plot_from=None, plot_every=1, plot_until=None, save_J=False, add_space=None,
-                  use_field_monitor=False, field_monitor=None, use_edt=None, **kwargs):
+                  use_field_monitor=False, field_monitor=None, use_edt=None, save_Ez=False, **kwargs):
+        """The reference's wakesolve (wakis/routines.py:231-485).  The Ez line history the
+        reference always writes to Ez.h5 is recorded on the device only with save_Ez=True
+        and written to wake.Ez_file at the end (HDF5 with the reference's datasets when
+        h5py is importable, else an .npz archive with the same keys); the wake potential
+        itself comes from the device taps either way."""
         if wake is not None:
             self.wake = wake
         if self.wake is None:
@@ -144,6 +150,7 @@ class RoutinesMixin:
                                       "E-pass kernel and not stored")
         wake = self.wake
         beam, Nt = self._wake_prepare(wake, wakelength, compute_plane)
+        hist = self._start_ez_record(wake, Nt) if save_Ez and Nt > 0 else None
         if self.verbose:
             print("Running electromagnetic time-domain simulation...")
         t0 = time.time()
@@ -173,6 +180,9 @@ class RoutinesMixin:
                 if callback is not None:
                     callback(self, n * self.dt)
         self.simulationTime = time.time() - t0
+        if hist is not None:
+            self._ctx.call("fit_set_ez_record", None, 0, None, None, 0, 0)
+            self._write_ez(wake, hist, Nt)
         wake.solve(compute_plane=compute_plane)
         self.logger.wakeSolver = wake.logger.wakeSolver
         self.logger.wakeSolver["wakelength"] = wakelength
@@ -232,6 +242,41 @@ class RoutinesMixin:
         self._after_device_run()
 
     # ------------------------------------------------------------------ helpers
+    def _start_ez_record(self, wake, Nt):
+        """Device buffer (Nt, lines, Nz) of E_z on the wake's integration lines, filled by
+        the step prologue before every step."""
+        lines = wake._run["lines"]
+        hist = torch.empty((Nt, len(lines), self.Nz), dtype=self.E.array.dtype, device=self.E.array.device)
+        lx = np.ascontiguousarray([l[0] for l in lines], dtype=np.int32)
+        ly = np.ascontiguousarray([l[1] for l in lines], dtype=np.int32)
+        self._ctx.call("fit_set_ez_record", nat.C.c_void_p(hist.data_ptr()), len(lines), nat.iptr32(lx),
+                       nat.iptr32(ly), 0, int(Nt))
+        return hist
+
+    def _write_ez(self, wake, hist, Nt):
+        """Ez.h5 datasets of the reference (x, y, z, dx, dy, dz, t and one slab per step,
+        '#00000' ...; a slab is E[xx, yy, :, 'z'], shape (3, 3, Nz) or (Nz,))."""
+        slabs = hist.cpu().numpy()
+        shape = (3, 3, self.Nz) if slabs.shape[1] == 9 else (self.Nz,)
+        data = {"x": wake.xf, "y": wake.yf, "z": wake.zf, "dx": self.grid.dx, "dy": self.grid.dy,
+                "dz": self.grid.dz, "t": wake.t}
+        for n in range(Nt):
+            data["#" + str(n).zfill(5)] = slabs[n].reshape(shape)
+        try:
+            import h5py
+        except ImportError:
+            h5py = None
+        fname = wake.Ez_file
+        if h5py is not None:
+            with h5py.File(fname, "w") as hf:
+                for k, v in data.items():
+                    hf[k] = v
+        else:
+            if fname.endswith(".h5"):
+                fname = fname[:-3] + ".npz"
+            np.savez(fname, **data)
+        wake.Ez_file = fname
+
     def _attach_monitor(self, monitor, n0, nsteps):
         """FieldMonitor as the epilogue of device-loop steps n0 .. n0+nsteps-1: the phase
         table continues the monitor's own time index."""

@@ -96,7 +96,7 @@ class WakeSolver:
         lx = np.ascontiguousarray([a for a, _ in lines], dtype=np.int32)
         ly = np.ascontiguousarray([b for _, b in lines], dtype=np.int32)
         dzt = np.ascontiguousarray(self.dz[:nz], dtype=np.float64)
-        self._run = dict(solver=solver, s=s, nlines=len(lines), longitudinal=longitudinal,
+        self._run = dict(solver=solver, s=s, nlines=len(lines), lines=list(lines), longitudinal=longitudinal,
                          keep=(lx, ly, row_ptr, em, ek0, ecnt, dzt))
         solver._ctx.call("fit_set_wake_taps", len(lines), nat.iptr32(lx), nat.iptr32(ly), int(kskip), len(s),
                          int(nsteps), nat.iptr64(row_ptr), nat.iptr32(em), nat.iptr32(ek0), nat.iptr32(ecnt),
@@ -350,6 +350,33 @@ class WakeSolver:
         wake = np.real(-1 * np.fft.fft(Z, n=samples))
         wake = np.roll(wake, -1)
         return [np.linspace(0, tmax, len(wake)), wake]
+
+    def read_Ez(self, filename=None, return_value=False):
+        """Opens an Ez line history (wakis/wakeSolver.py:1317-1364): an HDF5 file as the
+        reference writes it, or the .npz archive with the same keys that
+        SolverFIT3D.wakesolve(save_Ez=True) writes without h5py.  Sets xf, yf, zf, dx, dy,
+        dz and t; the per-step slabs '#00000', ... stay in Ez_hf."""
+        if filename is None:
+            filename = self.Ez_file
+        if str(filename).endswith(".npz"):
+            hf = np.load(filename)
+        else:
+            try:
+                import h5py
+            except ImportError:
+                raise ImportError("reading an HDF5 Ez file needs h5py; wakesolve(save_Ez=True) writes an .npz "
+                                  "archive with the same keys when h5py is missing") from None
+            hf = h5py.File(filename, "r")
+        self.log(f"Reading Ez file {filename}")
+        self.Ez_hf = hf
+        self.Ez_file = filename
+        keys = set(hf.keys())
+        for key, attr in (("x", "xf"), ("y", "yf"), ("z", "zf"), ("dx", "dx"), ("dy", "dy"), ("dz", "dz"),
+                          ("t", "t")):
+            if key in keys:
+                setattr(self, attr, np.array(hf[key]))
+        if return_value:
+            return hf
 
     def read_txt(self, txt, skiprows=2, delimiter=None, usecols=None):
         try:
