@@ -40,7 +40,7 @@ def assert_same(got, ref):
 
 
 def test_pooled_mix_matches_wakesolve(alone):
-    loop = S.ServingLoop(budget_bytes=8 << 30, chunk_steps=16)
+    loop = S.ServingLoop(budget_bytes=8 << 30, chunk_steps=16, kernels="direct")
     try:
         recs, summ = loop.run(small_requests())
     finally:
@@ -52,10 +52,12 @@ def test_pooled_mix_matches_wakesolve(alone):
 
 
 def test_pooled_results_match_the_default_wakesolve_to_rounding():
-    for req in small_requests()[:2]:
-        ref = S.solve_alone(req, np.float32)  # default kernels (fused where it applies)
+    """The pool's fused kernel (kernels='auto': even Nx) against the default wakesolve
+    (the single-grid fused kernel there); odd Nx runs the two-pass kernels on both sides."""
+    for req in small_requests():
+        ref = S.solve_alone(req, np.float32)
         pool = nat.Pool(1 << 30, chunk_steps=32)
-        job = S.ServedSolve(req)
+        job = S.ServedSolve(req, kernels="auto")
         try:
             job.submit(pool)
             while not pool.poll(wait_ms=100):
@@ -71,7 +73,7 @@ def test_pooled_results_match_the_default_wakesolve_to_rounding():
 
 def test_solves_submitted_together_share_chunks(alone):
     """All solves built first, then submitted back to back: they run in the same chunks."""
-    jobs = [S.ServedSolve(r) for r in small_requests()]
+    jobs = [S.ServedSolve(r, kernels="direct") for r in small_requests()]
     pool = nat.Pool(8 << 30, chunk_steps=8)
     try:
         for j in jobs:
@@ -92,8 +94,8 @@ def test_solves_submitted_together_share_chunks(alone):
 
 def test_one_at_a_time_budget_gives_the_same_results(alone):
     reqs = small_requests()
-    biggest = max(S.footprint_bytes(r) for r in reqs)
-    loop = S.ServingLoop(budget_bytes=biggest, chunk_steps=64)
+    biggest = max(S.footprint_bytes(r, kernels="direct") for r in reqs)
+    loop = S.ServingLoop(budget_bytes=biggest, chunk_steps=64, kernels="direct")
     try:
         recs, summ = loop.run(reqs)
     finally:
@@ -108,7 +110,7 @@ def test_staggered_arrivals_join_running_solves(alone):
     reqs = small_requests()
     for i, r in enumerate(reqs):
         r.arrival = 0.02 * i
-    loop = S.ServingLoop(budget_bytes=8 << 30, chunk_steps=4)
+    loop = S.ServingLoop(budget_bytes=8 << 30, chunk_steps=4, kernels="direct")
     try:
         recs, summ = loop.run(reqs)
     finally:
@@ -157,3 +159,30 @@ def test_pool_rejects_fp64_contexts():
     finally:
         pool.close()
         job.close()
+
+
+def test_fused_pool_mix_with_odd_step_counts():
+    """Fused rows (even Nx) next to two-pass rows in one mix, chunk lengths that end
+    instances inside a chunk, odd step counts (the first step is taken at submission):
+    every result agrees with its default wakesolve to rounding."""
+    reqs = small_requests()
+    refs = {r.tag: S.solve_alone(r, np.float32) for r in reqs}
+    jobs = [S.ServedSolve(r, kernels="auto") for r in reqs]
+    assert [j.solver.kernels for j in jobs] == ["fused", "fused", "direct", "fused"]
+    pool = nat.Pool(8 << 30, chunk_steps=6)
+    try:
+        for j in jobs:
+            j.submit(pool)
+        done = []
+        while len(done) < len(jobs):
+            done += pool.poll(wait_ms=100)
+    finally:
+        pool.close()
+    assert all(d["status"] == 0 for d in done)
+    assert {d["tag"]: d["steps"] for d in done} == {j.req.tag: j.Nt - j.first for j in jobs}
+    for j in jobs:
+        got = j.finish()
+        for k in ("WP", "Z", "WPx"):
+            a, b = np.asarray(got[k]), np.asarray(refs[j.req.tag][k])
+            assert np.linalg.norm(a - b) <= 1e-5 * max(np.linalg.norm(b), 1e-30), (j.req.tag, k)
+        j.close()

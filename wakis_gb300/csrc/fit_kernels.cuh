@@ -684,21 +684,21 @@ struct FusedShared {
 template <int FY>
 constexpr int fused_min_blocks() { return FY >= 8 ? 2 : 3; }
 
+// The march of one tile column (bx, by) through planes k0 .. k1-1 (all threads of the
+// CTA call it; the plane buffers in sm are free on entry).
 template <typename T, int VEC, int FY, int MODE>
-__global__ void __launch_bounds__(32 * (FY + 1), fused_min_blocks<FY>())
-    k_step_fused(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout, T* __restrict__ Hout,
-                 const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl, T* __restrict__ J,
-                 int use_cond, Geom g, Metric<T> mt, BeamArgs b, StepArgs st, int zlen) {
+__device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout,
+                                            T* __restrict__ Hout, const T* __restrict__ ch, const T* __restrict__ ce,
+                                            const T* __restrict__ cl, T* __restrict__ J, int use_cond, const Geom& g,
+                                            const Metric<T>& mt, const BeamArgs& b, const StepArgs& st, int bx, int by,
+                                            int k0, int k1, FusedShared<T, VEC, FY>& sm) {
     constexpr int FX = 32 * VEC;
-    __shared__ FusedShared<T, VEC, FY> sm;
     const int lane = threadIdx.x, ty = threadIdx.y;
     const bool halo = ty == FY;  // the halo warp
-    const int i0 = blockIdx.x * FX + lane * VEC;
-    const int jt = blockIdx.y * FY;           // first row of the tile
+    const int i0 = bx * FX + lane * VEC;
+    const int jt = by * FY;                   // first row of the tile
     const int j = halo ? jt : jt + ty;        // the halo warp works below row jt
     const bool on = i0 < g.nx && j < g.ny;
-    const int k0 = blockIdx.z * zlen;
-    const int k1 = min(g.nz, k0 + zlen);
     const PlaneArgs pl{};
     const int xo = lane * VEC;
     if (k0 > 0 && on && !halo) {  // new H of plane k0-1 (the plane below the range) for the tile
@@ -742,7 +742,7 @@ __global__ void __launch_bounds__(32 * (FY + 1), fused_min_blocks<FY>())
                 }
             }
             // the cell before each row segment: flat n - 1 (may wrap)
-            const int ib = blockIdx.x * FX;
+            const int ib = bx * FX;
             if (lane < FY && ib < g.nx && jt + lane < g.ny) {
                 const long long m = (long long)ib + g.sy * (jt + lane) + g.sz * k - 1;
                 T ax[1], ay[1], az[1];
@@ -811,6 +811,17 @@ __global__ void __launch_bounds__(32 * (FY + 1), fused_min_blocks<FY>())
             st_v<T, VEC>(Eout + 2 * g.N + n, ez);
         }
     }
+}
+
+template <typename T, int VEC, int FY, int MODE>
+__global__ void __launch_bounds__(32 * (FY + 1), fused_min_blocks<FY>())
+    k_step_fused(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout, T* __restrict__ Hout,
+                 const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl, T* __restrict__ J,
+                 int use_cond, Geom g, Metric<T> mt, BeamArgs b, StepArgs st, int zlen) {
+    __shared__ FusedShared<T, VEC, FY> sm;
+    const int k0 = blockIdx.z * zlen;
+    fused_march<T, VEC, FY, MODE>(Ein, Hin, Eout, Hout, ch, ce, cl, J, use_cond, g, mt, b, st, blockIdx.x, blockIdx.y,
+                                  k0, min(g.nz, k0 + zlen), sm);
 }
 
 // ---------------------------------------------------------------- staged kernels
@@ -1479,8 +1490,14 @@ __global__ void k_dft_reduce(const double2* __restrict__ part, int nsig, int nb,
 // pooled instance gives bit-identical fields to the same grid run alone.
 constexpr int kPoolMaxInst = 64;
 constexpr int kPoolTpb = 256;
+// classes: 0, 1, 2 = two-pass kernels with 4-, 2-, 1-wide vectors; 3, 4 = the fused step
+// with 4- and 2-wide vectors (contexts with the fused step enabled and Nx even)
+constexpr int kPoolClasses = 5;
+constexpr int kPoolFusedRows = 4;   // rows per fused tile (plus the halo warp)
+constexpr int kPoolFusedZlen = 32;  // planes per fused work item
 
 __host__ __device__ constexpr int pool_class(int vec) { return vec == 4 ? 0 : (vec == 2 ? 1 : 2); }
+__host__ __device__ constexpr int pool_fused_class(int vec) { return vec == 4 ? 3 : 4; }
 
 template <typename T>
 struct PoolInst {
@@ -1498,20 +1515,24 @@ struct PoolInst {
     const double* vt_table;
     long long vt_len;
     long long n_end;  // steps n < n_end are taken
-    long long tile0;  // first tile of the instance
-    long long ntile;  // tiles of the instance: ceil(nvec / kPoolTpb)
+    long long tile0;  // first tile (fused: work item) of the instance in its class
+    long long ntile;  // tiles: ceil(nvec / kPoolTpb); fused: tiles_x * tiles_y * z ranges
     long long nvec;   // N / vec
+    T* E2;            // fused: the second field buffers (steps alternate E,H <-> E2,H2)
+    T* H2;
     int vec;          // cells per vector: 4, 2 or 1 (Nx % vec == 0)
     int mode;         // 0: lossless, 1: J = sigma*E folded into the loss factor
     int use_cond;
-    int pad;
+    int fused;        // 1: stepped by k_step_fused_pool
+    int tiles_x, tiles_y;  // fused tile grid of one z range
+    int pad0, pad1;
 };
 
 template <typename T>
 struct PoolTable {
     int ninst;
     int pad;
-    long long cls_t0[4];  // tiles of class c: [cls_t0[c], cls_t0[c+1])
+    long long cls_t0[kPoolClasses + 1];  // tiles (work items) of class c: [cls_t0[c], cls_t0[c+1])
     PoolInst<T> inst[kPoolMaxInst];
 };
 
@@ -1593,14 +1614,56 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T
     });
 }
 
-// one block per table row: wake taps of E^n and the step counter (advanced past the
-// end too, so the passes of this step see n >= n_end and skip the finished instance)
+// The fused step of every instance of one fused class: work items (a tile column and a
+// range of kPoolFusedZlen planes of one instance) in grid-stride order, each marched by
+// fused_march, the code of the single-grid fused kernel.  dir = 0 steps (E, H) ->
+// (E2, H2), dir = 1 back: every fused instance enters a chunk with its state in (E, H)
+// and takes an even number of steps in it, so all of them share the direction of a step.
+template <typename T, int VEC>
+__global__ void __launch_bounds__(32 * (kPoolFusedRows + 1), 3) k_step_fused_pool(const PoolTable<T>* __restrict__ tab,
+                                                                               int dir) {
+    __shared__ FusedShared<T, VEC, kPoolFusedRows> sm;
+    __shared__ PoolInst<T> si;
+    __shared__ long long sn;
+    const int ninst = tab->ninst;
+    const long long c0 = tab->cls_t0[pool_fused_class(VEC)], c1 = tab->cls_t0[pool_fused_class(VEC) + 1];
+    for (long long w = c0 + blockIdx.x; w < c1; w += gridDim.x) {
+        __syncthreads();  // the previous work item no longer reads sm or si
+        pool_fetch<T>(tab, ninst, w, &si, &sn);
+        __syncthreads();
+        if (sn >= si.n_end) continue;
+        const long long local = w - si.tile0;
+        const long long per_z = (long long)si.tiles_x * si.tiles_y;
+        const int bz = (int)(local / per_z);
+        const int rem = (int)(local - bz * per_z);
+        const int by = rem / si.tiles_x, bx = rem - by * si.tiles_x;
+        const int k0 = bz * kPoolFusedZlen, k1 = min(si.g.nz, k0 + kPoolFusedZlen);
+        const T* Ein = dir ? si.E2 : si.E;
+        const T* Hin = dir ? si.H2 : si.H;
+        T* Eout = dir ? si.E : si.E2;
+        T* Hout = dir ? si.H : si.H2;
+        StepArgs st{};
+        st.d_step = si.d_step;
+        st.vt_table = si.vt_table;
+        st.vt_len = si.vt_len;
+        if (si.mode == 1)
+            fused_march<T, VEC, kPoolFusedRows, 1>(Ein, Hin, Eout, Hout, si.ch, si.ce, si.cl, si.J, si.use_cond, si.g,
+                                                   si.mt, si.beam, st, bx, by, k0, k1, sm);
+        else
+            fused_march<T, VEC, kPoolFusedRows, 0>(Ein, Hin, Eout, Hout, si.ch, si.ce, si.cl, si.J, si.use_cond, si.g,
+                                                   si.mt, si.beam, st, bx, by, k0, k1, sm);
+    }
+}
+
+// one block per table row: wake taps of E^n (read from the buffer holding the state:
+// the second one on odd steps of a fused instance) and the step counter (advanced past
+// the end too, so the passes of this step see n >= n_end and skip the finished instance)
 template <typename T>
-__global__ void k_prologue_pool(const PoolTable<T>* __restrict__ tab) {
+__global__ void k_prologue_pool(const PoolTable<T>* __restrict__ tab, int dir) {
     if ((int)blockIdx.x >= tab->ninst) return;
     const PoolInst<T>& d = tab->inst[blockIdx.x];
     const long long n = *d.d_step;
-    if (n < d.n_end) wake_taps<T>(d.E, d.g, d.tap, n);
+    if (n < d.n_end) wake_taps<T>((d.fused && dir) ? d.E2 : d.E, d.g, d.tap, n);
     __syncthreads();
     if (threadIdx.x == 0) *d.d_step = n + 1;
 }

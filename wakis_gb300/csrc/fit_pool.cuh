@@ -31,6 +31,7 @@ struct PoolSlot {
     cudaEvent_t ready = nullptr;  // end of the caller's work on the context before submit
     bool joined = false;          // the pool stream has waited on `ready`
     double t_submit = 0.0, t_start = -1.0;
+    long long pre_steps = 0;  // steps taken at submission (the odd first step of a fused context)
 };
 
 struct InFlight {
@@ -48,13 +49,14 @@ struct FitPool {
     int ctas_per_sm = 0;
     int minb[3]{3, 3, 4};          // kernel variant (CTAs per SM of its register budget) per class
     int grid_h[3]{}, grid_e[3]{};  // persistent CTAs of the pass kernels per vector class
+    int grid_f[2]{};               // persistent CTAs of the fused kernels (4-, 2-wide vectors)
     int gen = 0;                   // bumped by fit_pool_tune: captured graphs of older variants are stale
     cudaStream_t ps = nullptr;     // every chunk runs here
     cudaEvent_t ev[2]{};
     PoolTable<float>* d_tab[2]{};
     PoolTable<float>* h_tab[2]{};
-    cudaGraphExec_t graph[2][8]{};  // [table][mask of the classes present]
-    int graph_gen[2][8]{};
+    cudaGraphExec_t graph[2][1 << kPoolClasses]{};  // [table][mask of the classes present]
+    int graph_gen[2][1 << kPoolClasses]{};
     long long budget = 0, reserved = 0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -97,7 +99,7 @@ void finish_slot(FitPool* p, PoolSlot* s, int status, double t) {
     // caller holds p->mu
     FitPoolDone d{};
     d.tag = s->tag;
-    d.steps = status == FIT_OK ? s->nsteps : 0;
+    d.steps = status == FIT_OK ? s->nsteps + s->pre_steps : 0;
     d.status = status;
     d.t_submit_ms = s->t_submit;
     d.t_start_ms = s->t_start;
@@ -129,10 +131,11 @@ int stage_table(FitPool* p, int b, const std::vector<PoolSlot*>& members) {
     PoolTable<float>* t = p->h_tab[b];
     long long tile = 0;
     int n = 0, mask = 0;
-    for (int cls = 0; cls < 3; ++cls) {
+    for (int cls = 0; cls < kPoolClasses; ++cls) {
         t->cls_t0[cls] = tile;
         for (PoolSlot* s : members) {
-            if (pool_class(s->row.vec) != cls) continue;
+            const int sc = s->row.fused ? pool_fused_class(s->row.vec) : pool_class(s->row.vec);
+            if (sc != cls) continue;
             PoolInst<float>& r = t->inst[n++];
             r = s->row;
             r.tile0 = tile;
@@ -140,7 +143,7 @@ int stage_table(FitPool* p, int b, const std::vector<PoolSlot*>& members) {
             mask |= 1 << cls;
         }
     }
-    t->cls_t0[3] = tile;
+    t->cls_t0[kPoolClasses] = tile;
     t->ninst = n;
     return mask;
 }
@@ -175,7 +178,7 @@ cudaError_t pool_grids(int nsm, int cls, int minb, int ctas_per_sm, int* gh, int
 }
 
 struct PoolTune {
-    int minb[3], grid_h[3], grid_e[3], gen;
+    int minb[3], grid_h[3], grid_e[3], grid_f[2], gen;
 };
 
 // kernel entry of class cls's pass with variant m
@@ -192,13 +195,11 @@ const void* pool_pass_func(int cls, int m, bool e_pass) {
 
 // appends one kernel node after *prev (graphs are built node by node, not captured, so
 // building one never interferes with device-wide synchronisation by other threads)
-cudaError_t add_node(cudaGraph_t g, cudaGraphNode_t* prev, const void* func, int grid, int block,
-                     PoolTable<float>* tab) {
-    void* args[1] = {&tab};
+cudaError_t add_node(cudaGraph_t g, cudaGraphNode_t* prev, const void* func, int grid, dim3 block, void** args) {
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(func);
     kp.gridDim = dim3((unsigned)grid);
-    kp.blockDim = dim3((unsigned)block);
+    kp.blockDim = block;
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
     kp.extra = nullptr;
@@ -209,7 +210,8 @@ cudaError_t add_node(cudaGraph_t g, cudaGraphNode_t* prev, const void* func, int
 }
 
 // the graph of table b with the classes in mask: chunk_steps x [taps + counters, the H
-// pass of each class present, the E pass of each class present]
+// pass of each two-pass class present, their E passes, the fused step of each fused
+// class present (direction alternating with the step)]
 cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraphExec_t* out) {
     if (p->graph[b][mask] && p->graph_gen[b][mask] == t.gen) {
         *out = p->graph[b][mask];
@@ -222,13 +224,23 @@ cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraph
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaGraphCreate(&gr, 0);
     cudaGraphNode_t prev = nullptr;
+    PoolTable<float>* tab = p->d_tab[b];
     for (int s = 0; s < p->chunk && e == cudaSuccess; ++s) {
-        e = add_node(gr, &prev, (const void*)k_prologue_pool<float>, kPoolMaxInst, 256, p->d_tab[b]);
+        int dir = s & 1;
+        void* pro_args[2] = {&tab, &dir};
+        e = add_node(gr, &prev, (const void*)k_prologue_pool<float>, kPoolMaxInst, dim3(256), pro_args);
+        void* pass_args[1] = {&tab};
         for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass)
             for (int cls = 0; cls < 3 && e == cudaSuccess; ++cls)
                 if (mask & (1 << cls))
                     e = add_node(gr, &prev, pool_pass_func(cls, t.minb[cls], pass == 1),
-                                 pass == 1 ? t.grid_e[cls] : t.grid_h[cls], kPoolTpb, p->d_tab[b]);
+                                 pass == 1 ? t.grid_e[cls] : t.grid_h[cls], dim3(kPoolTpb), pass_args);
+        void* fused_args[2] = {&tab, &dir};
+        const dim3 fused_block(32, kPoolFusedRows + 1);  // lanes along x, one warp per row + the halo warp
+        if (e == cudaSuccess && (mask & (1 << 3)))
+            e = add_node(gr, &prev, (const void*)k_step_fused_pool<float, 4>, t.grid_f[0], fused_block, fused_args);
+        if (e == cudaSuccess && (mask & (1 << 4)))
+            e = add_node(gr, &prev, (const void*)k_step_fused_pool<float, 2>, t.grid_f[1], fused_block, fused_args);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b][mask], gr, 0);
     if (gr) cudaGraphDestroy(gr);
@@ -239,7 +251,14 @@ cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraph
     return e;
 }
 
-int popcount3(int m) { return (m & 1) + ((m >> 1) & 1) + ((m >> 2) & 1); }
+// kernel launches of one step of a chunk with the classes in mask
+int pool_launches_per_step(int mask) {
+    int n = 1;
+    for (int c = 0; c < 3; ++c) n += 2 * ((mask >> c) & 1);
+    for (int c = 3; c < kPoolClasses; ++c) n += (mask >> c) & 1;
+    return n;
+}
+
 
 void pool_main(FitPool* p) {
     if (cudaSetDevice(p->device) != cudaSuccess) {
@@ -273,6 +292,8 @@ void pool_main(FitPool* p) {
                     tune.grid_h[c] = p->grid_h[c];
                     tune.grid_e[c] = p->grid_e[c];
                 }
+                tune.grid_f[0] = p->grid_f[0];
+                tune.grid_f[1] = p->grid_f[1];
                 tune.gen = p->gen;
             }
         }
@@ -295,7 +316,7 @@ void pool_main(FitPool* p) {
                 pool_abort(p, e, "pool chunk launch");
                 break;
             }
-            g_launches += (1LL + 2LL * popcount3(mask)) * p->chunk;
+            g_launches += (long long)pool_launches_per_step(mask) * p->chunk;
             InFlight f;
             f.buf = b;
             f.t_launch = p->now();
@@ -353,7 +374,7 @@ void pool_free(FitPool* p) {
     cudaSetDevice(p->device);
     if (p->ps) cudaStreamSynchronize(p->ps);
     for (int b = 0; b < 2; ++b) {
-        for (int m = 0; m < 8; ++m)
+        for (int m = 0; m < (1 << kPoolClasses); ++m)
             if (p->graph[b][m]) cudaGraphExecDestroy(p->graph[b][m]);
         if (p->ev[b]) cudaEventDestroy(p->ev[b]);
         if (p->d_tab[b]) cudaFree(p->d_tab[b]);
@@ -387,6 +408,13 @@ int fit_pool_create(int32_t device, int64_t budget_bytes, int32_t chunk_steps, i
     p->ctas_per_sm = ctas_per_sm;
     for (int c = 0; c < 3 && e == cudaSuccess; ++c)
         e = pool_grids(p->nsm, c, p->minb[c], ctas_per_sm, &p->grid_h[c], &p->grid_e[c]);
+    int of4 = 0, of2 = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&of4, k_step_fused_pool<float, 4>, 32 * (kPoolFusedRows + 1), 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&of2, k_step_fused_pool<float, 2>, 32 * (kPoolFusedRows + 1), 0);
+    p->grid_f[0] = p->nsm * std::max(of4, 1);
+    p->grid_f[1] = p->nsm * std::max(of2, 1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->ps, cudaStreamNonBlocking);
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         e = cudaEventCreateWithFlags(&p->ev[b], cudaEventDisableTiming | cudaEventBlockingSync);
@@ -476,6 +504,16 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     static thread_local long long host_n0;
     host_n0 = n0;
     CK(cudaMemcpyAsync(c->d_step, &host_n0, sizeof(long long), cudaMemcpyHostToDevice, c->own));
+    // a context with the fused step enabled is stepped by the pooled fused kernel; it
+    // takes its steps in pairs (ending in E, H), so an odd count takes its first step
+    // here with the two-pass kernels
+    const int mode = c->use_cond ? 1 : 0;
+    const bool fused = fused_ok(c, mode);
+    long long pooled = nsteps;
+    if (fused && (nsteps % 2)) {
+        launch_step(c, 0, mode, true);
+        pooled -= 1;
+    }
     PoolSlot* s = new PoolSlot();
     cudaError_t e = cudaEventCreateWithFlags(&s->ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(s->ready, c->own);
@@ -487,7 +525,8 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     }
     s->c = c;
     s->tag = tag;
-    s->nsteps = nsteps;
+    s->nsteps = pooled;
+    s->pre_steps = nsteps - pooled;
     PoolInst<float>& r = s->row;
     r.g = c->g;
     r.mt = metric<float>(c);
@@ -508,6 +547,14 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     r.mode = c->use_cond ? 1 : 0;
     r.use_cond = c->use_cond;
     r.ntile = (r.nvec + kPoolTpb - 1) / kPoolTpb;
+    if (fused) {
+        r.fused = 1;
+        r.E2 = static_cast<float*>(c->E2);
+        r.H2 = static_cast<float*>(c->H2);
+        r.tiles_x = (c->g.nx + 32 * r.vec - 1) / (32 * r.vec);
+        r.tiles_y = (c->g.ny + kPoolFusedRows - 1) / kPoolFusedRows;
+        r.ntile = (long long)r.tiles_x * r.tiles_y * ((c->g.nz + kPoolFusedZlen - 1) / kPoolFusedZlen);
+    }
     s->ntiles = r.ntile;
     c->in_pool = true;
     {

@@ -84,15 +84,17 @@ def config3_requests(count=64, seed=3, rate_hz=None, wakelength=1.0):
     return out
 
 
-def footprint_bytes(req, dtype=np.float32):
+def footprint_bytes(req, dtype=np.float32, kernels="direct"):
     """Device bytes a request holds while it is served: E, H, J (3 x 3N field words), the
     FP64 material tensors ieps, imu, sigma (3 x 3N x 8), the library's coefficient arrays
-    (ch, ce and, with losses, cl: 3N field words each), the cell mask and a fixed
-    allowance for the 1-D metrics, tap tables and allocator rounding."""
+    (ch, ce and, with losses, cl: 3N field words each), with the fused step the second
+    E and H buffers (6N field words), the cell mask and a fixed allowance for the 1-D
+    metrics, tap tables and allocator rounding."""
     N = req.cells
     w = np.dtype(dtype).itemsize
     ncoef = 3 if req.lossy else 2
-    return int(N * (9 * w + 72 + 3 * w * ncoef + 1) + 8 * 2 ** 20)
+    fused = kernels == "fused" or (kernels == "auto" and req.n % 2 == 0)
+    return int(N * (9 * w + 72 + 3 * w * ncoef + 1 + (6 * w if fused else 0)) + 8 * 2 ** 20)
 
 
 def _axes(req):
@@ -150,10 +152,13 @@ def build(req, dtype=np.float32, device=0, results_folder=None, dt=None):
 class ServedSolve:
     """A request's solver between admission and its impedance."""
 
-    def __init__(self, req, dtype=np.float32, device=0, results_folder=None):
+    def __init__(self, req, dtype=np.float32, device=0, results_folder=None, kernels="direct"):
         self.req = req
         self.grid, self.wake, self.solver = build(req, dtype, device, results_folder)
         s = self.solver
+        # 'direct': the pool's two-pass kernels; 'fused' (or 'auto' with Nx even): the
+        # pool's fused kernel, which also holds the second E, H buffers
+        s.kernels = kernels
         self.beam, self.Nt = s._wake_prepare(self.wake, req.wakelength, "both")
         self.vt = s._wake_device_setup(self.beam, self.Nt)
         self.first = s._wake_first_step(self.beam)
@@ -194,10 +199,10 @@ def solve_alone(req, dtype=np.float32, device=0, dt=None, kernels="auto"):
 POOL_VARIANTS = {4: (2, 3), 2: (2, 3), 1: (3, 4)}
 
 
-def run_resident(pool, reqs):
+def run_resident(pool, reqs, kernels="direct"):
     """Builds every request, submits them together and waits: returns (cell-updates,
     seconds of pool time with chunks in flight, jobs)."""
-    jobs = [ServedSolve(r) for r in reqs]
+    jobs = [ServedSolve(r, kernels=kernels) for r in reqs]
     busy0 = pool.stats()["busy_ms"]
     for j in jobs:
         j.submit(pool)
@@ -242,7 +247,7 @@ def autotune(pool, calib=None, repeats=1):
             pool.tune(vec, minb)
             best = 0.0
             for _ in range(repeats):
-                cu, busy, jobs = run_resident(pool, reqs)
+                cu, busy, jobs = run_resident(pool, reqs, kernels="direct")
                 for j in jobs:
                     j.close()
                 del jobs
@@ -310,12 +315,13 @@ class ServingLoop:
     until it gets in (bounded waiting for large requests)."""
 
     def __init__(self, budget_bytes, chunk_steps=64, ctas_per_sm=0, device=0, dtype=np.float32, max_bypass=8,
-                 keep_results=True, variants=None):
+                 keep_results=True, variants=None, kernels="direct"):
         self.pool = nat.Pool(budget_bytes, chunk_steps=chunk_steps, ctas_per_sm=ctas_per_sm, device=device)
         for vec, minb in (variants or {}).items():
             self.pool.tune(vec, minb)
         self.device = device
         self.dtype = dtype
+        self.kernels = kernels
         self.admission = Admission(max_bypass)
         self.keep_results = keep_results
         self.results = {}
@@ -337,10 +343,10 @@ class ServingLoop:
             while pending and pending[0].arrival * time_scale <= now:
                 queue.append(pending.popleft())
             admitted = False
-            for req, nbytes in self.admission.admit(queue, lambda r: footprint_bytes(r, self.dtype),
+            for req, nbytes in self.admission.admit(queue, lambda r: footprint_bytes(r, self.dtype, self.kernels),
                                                     self.pool.reserve):
                 t_adm = time.perf_counter() - t0
-                job = ServedSolve(req, self.dtype, self.device, tmp)
+                job = ServedSolve(req, self.dtype, self.device, tmp, self.kernels)
                 job.submit(self.pool)
                 running[req.tag] = (job, nbytes, t_adm, time.perf_counter() - t0)
                 admitted = True
