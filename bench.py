@@ -225,6 +225,22 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def replica_max_ms(ms, device, world):
+    """The timed region's milliseconds, max over the ranks (a barrier first): the
+    replicas' job time."""
+    import torch
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells, steps, world, ms):
+    """Whole-job Mcell-updates/s: every rank steps its own full grid (weak scaling)."""
+    return cells * steps * world / (ms / 1e3) / 1e6
+
+
 def run_ours(args, rank, world):
     import torch
     import wakis_gb300 as wg
@@ -267,14 +283,9 @@ def run_ours(args, rank, world):
         ev1.record()
         torch.cuda.synchronize()
     launches = nat.launch_count() - launches0
-    ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], device=dev, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.barrier()
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = replica_max_ms(ev0.elapsed_time(ev1), dev, world)
     n += K
-    value = N * K * world / (ms / 1e3) / 1e6
+    value = replica_value(N, K, world, ms)
     # live per-kernel timing (same context, same stream)
     kt = np.zeros(2)
     s._ctx.call("fit_time_kernels", 10, nat.dptr(kt))
@@ -316,7 +327,7 @@ def run_ours(args, rank, world):
         shapes = {k: t for k, t in tuned.items() if k != "two-pass"}
         best = min(shapes, key=lambda t: shapes[t] if shapes[t] == shapes[t] else 0.0)
         out["fused_autotune"] = {"best": list(best),
-                                 "ms_per_step": {f"v{v}r{r}z{z}": t for (v, r, z), t in sorted(shapes.items())},
+                                 "ms_per_step": {f"v{v}r{r}z{z}c{m}": t for (v, r, z, m), t in sorted(shapes.items())},
                                  "two_pass_ms_per_step": tuned.get("two-pass")}
         out["config"]["kernels"] = "fused single-pass step (ping-pong field buffers)"
     else:
@@ -628,7 +639,7 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-no-fp64", action="store_true")
     ap.add_argument("--serve-no-saturated", action="store_true")
-    ap.add_argument("--fused-shape", type=int, nargs=3, default=None, metavar=("VEC", "ROWS", "ZSEG"),
+    ap.add_argument("--fused-shape", type=int, nargs=4, default=None, metavar=("VEC", "ROWS", "ZSEG", "CTAS"),
                     help="fused step tile shape (skips the autotuner)")
     ap.add_argument("--variant", default="auto", choices=["auto", "staged", "direct", "fused"],
                     help="step kernels: auto (the solver default: fused where it applies), direct H/E pass kernels, "

@@ -209,9 +209,10 @@ FIT_API int fit_check_error(FitCtx *ctx);
 FIT_API int fit_set_kernel_variant(FitCtx *ctx, int32_t variant);
 /* Tile shape of the fused step: vec cells per thread along x (2, or 4 for FP32; Nx must
  * be a multiple), rows (4 or 8) rows of 32 threads per CTA, zseg z ranges per tile
- * column (1..Nz).  fit_set_kernel_variant(ctx, 2) sets a default; the solver's
- * autotuner times the candidates on the grid itself with fit_time_fused. */
-FIT_API int fit_set_fused_shape(FitCtx *ctx, int32_t vec, int32_t rows, int32_t zseg);
+ * column (1..Nz), ctas the CTAs per SM its register budget is sized for (8 rows: 2;
+ * 4 rows: 3 or 4; 0 = the first).  fit_set_kernel_variant(ctx, 2) sets a default; the
+ * solver's autotuner times the candidates on the grid itself with fit_time_fused. */
+FIT_API int fit_set_fused_shape(FitCtx *ctx, int32_t vec, int32_t rows, int32_t zseg, int32_t ctas);
 /* Times, beam off, on the context stream between CUDA events: reps fused steps from
  * (E, H) into the second buffers (ms_out[0]), and reps two-pass steps (H pass + E pass)
  * in place on copies of E and H in the second buffers (ms_out[1]); average milliseconds

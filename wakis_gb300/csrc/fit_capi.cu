@@ -86,7 +86,7 @@ struct FitCtx {
     bool staged = false;    // staged (bulk-copy) passes when the grid is aligned (opt-in)
     bool fused = false;     // fused single-pass step in device loops (ping-pong with E2/H2)
     void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
-    int fused_vec = 4, fused_rows = 8, fused_zseg = 1;  // tile shape of the fused step
+    int fused_vec = 4, fused_rows = 8, fused_zseg = 1, fused_ctas = 2;  // tile shape of the fused step
     bool graph_fused = false;  // the cached graph holds fused steps
     RecordArgs rec{};           // Ez line history of recorded steps (nlines = 0: off)
     MonitorArgs mon{};          // field monitor epilogue of device-loop steps (nf = 0: off)
@@ -353,7 +353,7 @@ bool fused_ok(const FitCtx* c, int mode) {
     return c->fused && c->E2 && c->H2 && mode != 2 && !c->plane.active && !c->abc_axes && pick_vec(c) >= 2;
 }
 
-template <typename T, int VEC, int FY>
+template <typename T, int VEC, int FY, int MB>
 void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
     constexpr int FX = 32 * VEC;
     const T* Ein = static_cast<const T*>(forward ? c->E : c->E2);
@@ -369,33 +369,40 @@ void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, c
     const T* cl = static_cast<const T*>(c->cl);
     T* J = static_cast<T*>(c->J);
     if (mode == 1)
-        k_step_fused<T, VEC, FY, 1><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g,
-                                                              metric<T>(c), beam, st, zlen);
+        k_step_fused<T, VEC, FY, MB, 1><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond,
+                                                                  c->g, metric<T>(c), beam, st, zlen);
     else
-        k_step_fused<T, VEC, FY, 0><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g,
-                                                              metric<T>(c), beam, st, zlen);
+        k_step_fused<T, VEC, FY, MB, 0><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond,
+                                                                  c->g, metric<T>(c), beam, st, zlen);
     count(c);
 }
 
-// the fused step in the context's tile shape (fused_vec cells per thread, fused_rows rows)
+// the fused step in the context's tile shape: fused_vec cells per thread, fused_rows rows,
+// register budget for fused_ctas CTAs per SM (8 rows: 2; 4 rows: 3 or 4)
+template <typename T, int VEC>
+void launch_fused_vec(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
+    if (c->fused_rows == 8)
+        launch_fused_shape<T, VEC, 8, 2>(c, mode, st, forward, beam);
+    else if (c->fused_ctas == 4)
+        launch_fused_shape<T, VEC, 4, 4>(c, mode, st, forward, beam);
+    else
+        launch_fused_shape<T, VEC, 4, 3>(c, mode, st, forward, beam);
+}
+
 void launch_fused(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
-    const bool r8 = c->fused_rows == 8;
-    if (c->dtype == FIT_F64) {
-        r8 ? launch_fused_shape<double, 2, 8>(c, mode, st, forward, beam)
-           : launch_fused_shape<double, 2, 4>(c, mode, st, forward, beam);
-    } else if (c->fused_vec == 4) {
-        r8 ? launch_fused_shape<float, 4, 8>(c, mode, st, forward, beam)
-           : launch_fused_shape<float, 4, 4>(c, mode, st, forward, beam);
-    } else {
-        r8 ? launch_fused_shape<float, 2, 8>(c, mode, st, forward, beam)
-           : launch_fused_shape<float, 2, 4>(c, mode, st, forward, beam);
-    }
+    if (c->dtype == FIT_F64)
+        launch_fused_vec<double, 2>(c, mode, st, forward, beam);
+    else if (c->fused_vec == 4)
+        launch_fused_vec<float, 4>(c, mode, st, forward, beam);
+    else
+        launch_fused_vec<float, 2>(c, mode, st, forward, beam);
 }
 
 // default tile shape: the widest vector, 8 rows, z ranges for about four waves
 void fused_default_shape(FitCtx* c) {
     c->fused_vec = pick_vec(c) == 4 ? 4 : 2;
     c->fused_rows = 8;
+    c->fused_ctas = 2;
     const long long tiles = (long long)((c->g.nx + 32 * c->fused_vec - 1) / (32 * c->fused_vec)) *
                             ((c->g.ny + c->fused_rows - 1) / c->fused_rows);
     const long long want = (4LL * 2 * c->nsm + tiles - 1) / tiles;
@@ -1159,16 +1166,20 @@ int fit_set_kernel_variant(FitCtx* c, int32_t variant) {
     return FIT_OK;
 }
 
-int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg) {
+int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg, int32_t ctas) {
     if (!c) return FIT_ERR_ARG;
     if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     const bool vec_ok = (vec == 2 && c->g.nx % 2 == 0) || (vec == 4 && c->dtype == FIT_F32 && c->g.nx % 4 == 0);
-    if (!vec_ok || (rows != 4 && rows != 8) || zseg < 1 || zseg > c->g.nz)
-        return fail(c, FIT_ERR_ARG, "bad fused tile shape (vec %d, rows %d, z ranges %d)", vec, rows, zseg);
+    if (ctas == 0) ctas = rows == 8 ? 2 : 3;
+    const bool ctas_ok = (rows == 8 && ctas == 2) || (rows == 4 && (ctas == 3 || ctas == 4));
+    if (!vec_ok || !ctas_ok || zseg < 1 || zseg > c->g.nz)
+        return fail(c, FIT_ERR_ARG, "bad fused tile shape (vec %d, rows %d, z ranges %d, CTAs/SM %d)", vec, rows, zseg,
+                    ctas);
     invalidate(c);
     c->fused_vec = vec;
     c->fused_rows = rows;
     c->fused_zseg = zseg;
+    c->fused_ctas = ctas;
     return FIT_OK;
 }
 

@@ -681,9 +681,6 @@ struct FusedShared {
     T hx1[3][2][FY + 1];          // [plane buffer][Hy, Hz][row + 1]: the cell before each row segment
 };
 
-template <int FY>
-constexpr int fused_min_blocks() { return FY >= 8 ? 2 : 3; }
-
 // The march of one tile column (bx, by) through planes k0 .. k1-1 (all threads of the
 // CTA call it; the plane buffers in sm are free on entry).
 template <typename T, int VEC, int FY, int MODE>
@@ -813,8 +810,9 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
     }
 }
 
-template <typename T, int VEC, int FY, int MODE>
-__global__ void __launch_bounds__(32 * (FY + 1), fused_min_blocks<FY>())
+// MB: CTAs per SM the register budget is sized for (the launch bound)
+template <typename T, int VEC, int FY, int MB, int MODE>
+__global__ void __launch_bounds__(32 * (FY + 1), MB)
     k_step_fused(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout, T* __restrict__ Hout,
                  const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl, T* __restrict__ J,
                  int use_cond, Geom g, Metric<T> mt, BeamArgs b, StepArgs st, int zlen) {

@@ -205,10 +205,11 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
 
     def tune_fused(self, reps=5, zsegs=(2, 4, 8, 16, 32, 64, 128), force=False):
         """Autotuner of the fused step's tile shape for this grid: times every candidate
-        (cells per thread along x, rows per CTA, z ranges per tile column) with
+        (cells per thread along x, rows per CTA, z ranges per tile column, CTAs per SM of
+        the register budget) with
         fit_time_fused, which leaves E, H and J unchanged, keeps the fastest and
         remembers it for grids of the same shape (later calls reuse it unless force).
-        Returns {(vec, rows, zseg): ms}."""
+        Returns {(vec, rows, zseg, ctas): ms, 'two-pass': ms}."""
         if self._kernels != "fused":
             self.kernels = "fused"
         key = self._grid_key()
@@ -223,13 +224,13 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         times = {}
         ms = np.zeros(2)
         for vec in vecs:
-            for rows in (4, 8):
+            for rows, ctas in ((4, 3), (4, 4), (8, 2)):
                 for zseg in zsegs:
                     if zseg > self.Nz:
                         continue
-                    self._ctx.call("fit_set_fused_shape", vec, rows, zseg)
+                    self._ctx.call("fit_set_fused_shape", vec, rows, zseg, ctas)
                     self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
-                    times[(vec, rows, zseg)] = float(ms[0])
+                    times[(vec, rows, zseg, ctas)] = float(ms[0])
         times["two-pass"] = float(ms[1])
         best = min((t for t in times if t != "two-pass"), key=times.get)
         SolverFIT3D._fused_shapes[key] = (best, times)
