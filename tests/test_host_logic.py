@@ -162,3 +162,15 @@ def test_tap_table_reproduces_reference_loop(name):
     for m in range(len(sv)):
         ks = list(np.nonzero(valid[m])[0])
         assert seen.get(m, []) == ks
+
+
+def test_solver_without_a_device_raises_import_error():
+    """The reference raises ImportError when its GPU stack is missing
+    (wakis/solverFIT3D.py:365); a solver without a CUDA device does the same."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    import wakis_gb300 as wg
+    grid = wg.GridFIT3D(0, 1, 0, 1, 0, 1, 4, 4, 4, verbose=0)
+    with pytest.raises(ImportError):
+        wg.SolverFIT3D(grid, verbose=0)

@@ -45,7 +45,8 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self.verbose = verbose
         self.logger = Logger()
         if not torch.cuda.is_available():
-            raise RuntimeError("SolverFIT3D needs a CUDA device: the FIT kernels run on the GPU only")
+            # the reference raises ImportError when its GPU stack is missing (wakis/solverFIT3D.py:365)
+            raise ImportError("[!] no CUDA device: the wakis_gb300 FIT kernels run on the GPU only")
         if use_mpi:
             raise NotImplementedError("use_mpi: z-slab MPI decomposition is not provided")
         if use_conductors:
