@@ -66,6 +66,11 @@ class BCsMixin:
             if lo[a] == "abc" and hi[a] == "abc":
                 # the reference's snapshot dict of that axis loses its low entries
                 raise KeyError("xyz"[a] + "lo")
+        n = (self.Nx, self.Ny, self.Nz)
+        for a in range(3):
+            if lo[a] == "abc" and n[a] < 2:
+                # the reference's update copies plane 1 of that axis (wakis/boundaries.py:363-404)
+                raise IndexError(f"index 1 is out of bounds for axis {a} with size {n[a]}")
         return sum(1 << a for a in range(3) if lo[a] == "abc")
 
     def get_abc(self):
