@@ -36,7 +36,7 @@ def test_small_grid_against_oracle(shape, faces, dtype):
     x = np.cumsum(np.r_[0.0, rng.uniform(0.5, 1.5, nx)])
     y = np.cumsum(np.r_[0.0, rng.uniform(0.5, 1.5, ny)])
     z = np.cumsum(np.r_[0.0, rng.uniform(0.5, 1.5, nz)])
-    bg = [1.5, 1.0, 0.2]
+    bg = [1.5, 1.0, 1e-3]  # tau = eps/sigma stays above dt: a well-conditioned loss factor
     steps = 9
     s = wg.SolverFIT3D(wg.GridFIT3D(x=x, y=y, z=z, verbose=0), cfln=0.5, bc_low=lo, bc_high=hi, use_stl=False,
                        bg=bg, dtype=dtype, verbose=0)
