@@ -169,6 +169,21 @@ FIT_API int fit_materialize_J(FitCtx *ctx, const double *sigma, int32_t flags);
 FIT_API int fit_wake_finalize(FitCtx *ctx, double qscale, double ds, double dxf, double dyf,
                       double *wp3d, double *wpx, double *wpy);
 
+/* Wake potential from a recorded Ez line history, without a context: the post-processing
+ * of an Ez file (WakeSolver.calc_long_WP, wakis/wakeSolver.py:311-421, and
+ * calc_long_WP_3d + calc_trans_WP, wakis/wakeSolver.py:423-626).  Inputs (host):
+ * ezt (nlines*nz*nt FP64, line-major, each line the reference's Ezt (nz, nt)), it (nz*ns,
+ * z-major: the time index of tap (m, k) after the reference's negative-index wrap, -1
+ * where the reference skips the tap because it >= nt), dz (nz).  Per s index the sums run
+ * in the reference's order with plain FP64 adds of rounded products, continue from the
+ * previous line's result, and are divided by qscale after each line, so wp3d equals the
+ * reference's WP_3d bit for bit.  Then, for nlines == 9, the transverse wake as in
+ * fit_wake_finalize.  Outputs (host): wp3d (nlines*ns); wpx, wpy (ns each; untouched when
+ * nlines != 9 or NULL).  Errors: fit_last_error(NULL, ...). */
+FIT_API int fit_wake_history(const double *ezt, int32_t nlines, int64_t nt, int32_t nz, const int32_t *it,
+                             int32_t ns, const double *dz, double qscale, double ds, double dxf, double dyf,
+                             double *wp3d, double *wpx, double *wpy);
+
 /* FP64 direct DFT at bins b0 .. b0+nb-1 of an n-point zero-padded transform
  *   X_s[b] = sum_{t < len} x_s[t] exp(-2 pi i b t / n)
  * for nsig signals of length len (host, signal-major); out (host) holds nsig*nb

@@ -550,11 +550,14 @@ class OracleWake:
         self.lambdas = None
 
 
-def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=None, field_monitor=None):
+def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=None, field_monitor=None,
+              j_slabs=None):
     """Runs the time loop and returns the recorded Ez slab Ezs[n] = E_z(xx, yy, :) taken
     after the beam update and before the step (wakis/routines.py:438-448); a field
-    monitor is updated with E after each step (wakis/routines.py:450-451).  Then calls
-    the post-processing.  Returns the recorded slabs (float64)."""
+    monitor is updated with E after each step (wakis/routines.py:450-451).  With a list
+    j_slabs, the J_z slabs of the same lines are appended at the same point (the save_J
+    dump, wakis/routines.py:444-445).  Then calls the post-processing.  Returns the
+    recorded slabs (float64)."""
     if wakelength is None:
         wakelength = wake.wakelength
     ixt = np.abs(solver.x - wake.xtest).argmin()
@@ -577,6 +580,8 @@ def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=
     for n in range(Nt):
         beam.update(solver, n * solver.dt)
         slabs.append(np.array(ez[xx, yy, :], dtype=np.float64))
+        if j_slabs is not None:
+            j_slabs.append(np.array(solver.comp(solver.J, 2)[xx, yy, :], dtype=np.float64))
         solver.one_step()
         if field_monitor is not None:
             field_monitor.update(solver.E, solver.dt, solver.grid.shape)

@@ -79,6 +79,8 @@ _SIGS = {
     "fit_materialize_J": (_P, _P, C.c_int32),
     "fit_wake_finalize": (_P, C.c_double, C.c_double, C.c_double, C.c_double, _D, _D, _D),
     "fit_dft": (_D, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _D),
+    "fit_wake_history": (_D, C.c_int32, C.c_int64, C.c_int32, _I32, C.c_int32, _D, C.c_double, C.c_double,
+                         C.c_double, C.c_double, _D, _D, _D),
     "fit_time_kernels": (_P, C.c_int32, _D),
     "fit_check_error": (_P,),
     "fit_dft_noalloc": (_P, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, _P, _P),
@@ -171,6 +173,25 @@ def dft(signals, n, b0, nb):
     rc = load().fit_dft(dptr(x), x.shape[0], x.shape[1], int(n), int(b0), int(nb), dptr(out))
     check(rc)
     return out[..., 0] + 1j * out[..., 1]
+
+
+def wake_history(ezt, it, dz, qscale, ds=1.0, dxf=1.0, dyf=1.0):
+    """Wake integral of a recorded Ez line history on the device: ezt (nlines, nz, nt)
+    FP64, it (nz, ns) int32 (-1 = no tap), dz (nz,).  Returns (wp3d (nlines, ns), wpx,
+    wpy); wpx and wpy are None unless nlines == 9."""
+    ezt = np.ascontiguousarray(ezt, dtype=np.float64)
+    it = np.ascontiguousarray(it, dtype=np.int32)
+    dz = np.ascontiguousarray(dz, dtype=np.float64)
+    nl, nz, nt = ezt.shape
+    ns = it.shape[1]
+    if it.shape[0] != nz or dz.shape != (nz,):
+        raise ValueError("wake_history: shapes of ezt, it and dz do not agree")
+    wp3d = np.empty((nl, ns))
+    wpx, wpy = np.empty(ns), np.empty(ns)
+    rc = load().fit_wake_history(dptr(ezt), nl, nt, nz, iptr32(it), ns, dptr(dz), float(qscale), float(ds),
+                                 float(dxf), float(dyf), dptr(wp3d), dptr(wpx), dptr(wpy))
+    check(rc)
+    return (wp3d, wpx, wpy) if nl == 9 else (wp3d, None, None)
 
 
 class Context:

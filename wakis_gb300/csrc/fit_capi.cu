@@ -1041,6 +1041,64 @@ int fit_wake_finalize(FitCtx* c, double qscale, double ds, double dxf, double dy
     return leave(c);
 }
 
+int fit_wake_history(const double* ezt, int32_t nlines, int64_t nt, int32_t nz, const int32_t* it, int32_t ns,
+                     const double* dz, double qscale, double ds, double dxf, double dyf, double* wp3d, double* wpx,
+                     double* wpy) {
+    if (!ezt || !it || !dz || !wp3d || nlines <= 0 || nt <= 0 || nz <= 0 || ns <= 0 || nt > INT32_MAX)
+        return fail(nullptr, FIT_ERR_ARG, "bad fit_wake_history arguments");
+    const size_t n_ezt = (size_t)nlines * nz * nt, n_it = (size_t)nz * ns;
+    double *d_ezt = nullptr, *d_dz = nullptr, *d_wp = nullptr, *d_wpx = nullptr, *d_wpy = nullptr,
+           *d_scr = nullptr;
+    int* d_it = nullptr;
+    cudaStream_t s = nullptr;
+    auto cleanup = [&]() {
+        if (s) {
+            dfree(d_ezt, s);
+            dfree(d_dz, s);
+            dfree(d_wp, s);
+            dfree(d_wpx, s);
+            dfree(d_wpy, s);
+            dfree(d_scr, s);
+            dfree(d_it, s);
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    };
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) keep_freed_blocks(dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_ezt, n_ezt * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_it, n_it * sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_dz, (size_t)nz * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_wp, (size_t)nlines * ns * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_wpx, (size_t)ns * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_wpy, (size_t)ns * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_scr, 4 * (size_t)ns * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_ezt, ezt, n_ezt * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_it, it, n_it * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_dz, dz, (size_t)nz * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(nullptr, FIT_ERR_CUDA, "fit_wake_history setup failed: %s", cudaGetErrorString(e));
+    }
+    k_wake_history<<<(unsigned)((ns + 127) / 128), 128, 0, s>>>(d_ezt, nlines, nt, nz, d_it, ns, d_dz, qscale, d_wp);
+    k_wake_finalize<<<1, 1024, 0, s>>>(nullptr, nullptr, nlines, ns, qscale, ds, dxf, dyf, d_wp, d_wpx, d_wpy,
+                                       d_scr);
+    g_launches += 2;
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(wp3d, d_wp, (size_t)nlines * ns * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && nlines == 9 && wpx && wpy) {
+        e = cudaMemcpyAsync(wpx, d_wpx, (size_t)ns * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(wpy, d_wpy, (size_t)ns * sizeof(double), cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cleanup();
+    if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "fit_wake_history failed: %s", cudaGetErrorString(e));
+    return FIT_OK;
+}
+
 int fit_dft(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb, double* out) {
     if (!x || !out || nsig <= 0 || len <= 0 || n <= 0 || nb <= 0 || b0 < 0)
         return fail(nullptr, FIT_ERR_ARG, "bad fit_dft arguments");

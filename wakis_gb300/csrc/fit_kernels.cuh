@@ -1373,13 +1373,13 @@ __global__ void k_beam_line(T* __restrict__ J, Geom g, BeamArgs b, double vt) {
 
 // wake post-processing: combine lines with the non-reset accumulator of the reference,
 // then exclusive prefix sums (x ds) and the Panofsky-Wenzel central differences.
-// One block of 1024 threads.
+// One block of 1024 threads.  acc == nullptr: wp3d already holds the combined lines.
 __global__ void k_wake_finalize(const double* __restrict__ acc, const double* __restrict__ comp, int nlines,
                                 int ns, double qscale, double ds, double dxf, double dyf,
                                 double* __restrict__ wp3d, double* __restrict__ wpx, double* __restrict__ wpy,
                                 double* __restrict__ scratch /* 4*ns */) {
     // 1. line combination, sequential over lines, parallel over s
-    for (int m = threadIdx.x; m < ns; m += blockDim.x) {
+    for (int m = threadIdx.x; acc && m < ns; m += blockDim.x) {
         double prev = 0.0;
         for (int l = 0; l < nlines; ++l) {
             const double raw = acc[(long long)l * ns + m] + comp[(long long)l * ns + m];
@@ -1421,6 +1421,31 @@ __global__ void k_wake_finalize(const double* __restrict__ acc, const double* __
     for (int m = threadIdx.x; m < ns; m += blockDim.x) {
         wpx[m] = -(scratch[m] - scratch[ns + m]) / dxf;
         wpy[m] = -(scratch[2LL * ns + m] - scratch[3LL * ns + m]) / dyf;
+    }
+}
+
+// Wake integral from a recorded Ez line history, the post-processing of an Ez file
+// (wakis/wakeSolver.py:311-421 longitudinal, 423-551 over the 3x3 lines).  One thread
+// per s index m.  The reference's operation order is kept exactly: lines in order, k
+// ascending, plain FP64 sums of the rounded products Ez*dz (no FMA) continued from the
+// previous line's result (the accumulator is not reset), divided by q*1e12 after each
+// line.  ezt: [nlines][nz][nt], the reference's Ezt (nz, nt) per line; it: [nz][ns],
+// the time index of tap (m, k) or -1 where the reference skips it (it >= nt); entries
+// outside [0, nt) are skipped.
+__global__ void k_wake_history(const double* __restrict__ ezt, int nlines, long long nt, int nz,
+                               const int* __restrict__ it, int ns, const double* __restrict__ dz, double qscale,
+                               double* __restrict__ wp3d) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= ns) return;
+    double wp = 0.0;
+    for (int l = 0; l < nlines; ++l) {
+        const double* e = ezt + (long long)l * nz * nt;
+        for (int k = 0; k < nz; ++k) {
+            const int t = it[(long long)k * ns + m];
+            if (t >= 0 && t < nt) wp = __dadd_rn(wp, __dmul_rn(e[(long long)k * nt + t], dz[k]));
+        }
+        wp = __ddiv_rn(wp, qscale);
+        wp3d[(long long)l * ns + m] = wp;
     }
 }
 

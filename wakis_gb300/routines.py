@@ -134,7 +134,10 @@ class RoutinesMixin:
         reference always writes to Ez.h5 is recorded on the device only with save_Ez=True
         and written to wake.Ez_file at the end (HDF5 with the reference's datasets when
         h5py is importable, else an .npz archive with the same keys); the wake potential
-        itself comes from the device taps either way."""
+        itself comes from the device taps either way.  save_J writes the J_z slabs on the
+        same lines, taken after the beam update and before each step, to Jz.h5 (Jz.npz
+        without h5py) in the working directory, as the reference does; the steps then run
+        one by one from the host, as a callback makes them."""
         if wake is not None:
             self.wake = wake
         if self.wake is None:
@@ -145,9 +148,6 @@ class RoutinesMixin:
             self.wake.skip_cells = add_space
         if plot:
             raise NotImplementedError("plotting is not provided")
-        if save_J:
-            raise NotImplementedError("save_J writes Jz.h5 every step; the beam current is evaluated in the "
-                                      "E-pass kernel and not stored")
         wake = self.wake
         beam, Nt = self._wake_prepare(wake, wakelength, compute_plane)
         hist = self._start_ez_record(wake, Nt) if save_Ez and Nt > 0 else None
@@ -155,7 +155,12 @@ class RoutinesMixin:
             print("Running electromagnetic time-domain simulation...")
         t0 = time.time()
         monitor = field_monitor if (use_field_monitor and field_monitor is not None) else None
-        fast = callback is None and (monitor is None or isinstance(monitor, FieldMonitor))
+        fast = callback is None and not save_J and (monitor is None or isinstance(monitor, FieldMonitor))
+        jslabs = [] if save_J else None
+        if compute_plane.lower() == "longitudinal":
+            xx, yy = self.ixt, self.iyt
+        else:
+            xx, yy = slice(self.ixt - 1, self.ixt + 2), slice(self.iyt - 1, self.iyt + 2)
         if fast and Nt > 0:
             vt = self._wake_device_setup(beam, Nt)
             first = self._wake_first_step(beam)
@@ -174,6 +179,8 @@ class RoutinesMixin:
         else:
             for n in range(Nt):
                 beam.update(self, n * self.dt)
+                if jslabs is not None:
+                    jslabs.append(self.J[xx, yy, :, "z"])
                 self._advance(n)
                 if use_field_monitor and field_monitor is not None:
                     field_monitor.update(self.E, self.dt)
@@ -183,6 +190,8 @@ class RoutinesMixin:
         if hist is not None:
             self._ctx.call("fit_set_ez_record", None, 0, None, None, 0, 0)
             self._write_ez(wake, hist, Nt)
+        if jslabs is not None:
+            self._write_history("Jz.h5", wake, jslabs)
         wake.solve(compute_plane=compute_plane)
         self.logger.wakeSolver = wake.logger.wakeSolver
         self.logger.wakeSolver["wakelength"] = wakelength
@@ -254,19 +263,24 @@ class RoutinesMixin:
         return hist
 
     def _write_ez(self, wake, hist, Nt):
-        """Ez.h5 datasets of the reference (x, y, z, dx, dy, dz, t and one slab per step,
-        '#00000' ...; a slab is E[xx, yy, :, 'z'], shape (3, 3, Nz) or (Nz,))."""
+        """Ez.h5 of the reference from the device-recorded history (Nt, lines, Nz)."""
         slabs = hist.cpu().numpy()
         shape = (3, 3, self.Nz) if slabs.shape[1] == 9 else (self.Nz,)
+        wake.Ez_file = self._write_history(wake.Ez_file, wake, [slabs[n].reshape(shape) for n in range(Nt)])
+
+    def _write_history(self, fname, wake, slabs):
+        """A line-history file with the reference's datasets (wakis/routines.py:399-427):
+        x, y, z, dx, dy, dz, t and one slab per step, '#00000' ...; a slab is
+        F[xx, yy, :, 'z'], shape (3, 3, Nz) or (Nz,).  HDF5 when h5py is importable, else
+        an .npz archive with the same keys.  Returns the name written."""
         data = {"x": wake.xf, "y": wake.yf, "z": wake.zf, "dx": self.grid.dx, "dy": self.grid.dy,
                 "dz": self.grid.dz, "t": wake.t}
-        for n in range(Nt):
-            data["#" + str(n).zfill(5)] = slabs[n].reshape(shape)
+        for n, sl in enumerate(slabs):
+            data["#" + str(n).zfill(5)] = sl
         try:
             import h5py
         except ImportError:
             h5py = None
-        fname = wake.Ez_file
         if h5py is not None:
             with h5py.File(fname, "w") as hf:
                 for k, v in data.items():
@@ -275,7 +289,7 @@ class RoutinesMixin:
             if fname.endswith(".h5"):
                 fname = fname[:-3] + ".npz"
             np.savez(fname, **data)
-        wake.Ez_file = fname
+        return fname
 
     def _attach_monitor(self, monitor, n0, nsteps):
         """FieldMonitor as the epilogue of device-loop steps n0 .. n0+nsteps-1: the phase

@@ -102,9 +102,9 @@ class WakeSolver:
                          int(nsteps), nat.iptr64(row_ptr), nat.iptr32(em), nat.iptr32(ek0), nat.iptr32(ecnt),
                          int(nz), nat.dptr(dzt))
 
-    def _tap_index(self, nsaved, longitudinal, Nz):
-        """s and it(m, k) exactly as calc_long_WP_3d / calc_long_WP evaluate them
-        (wakis/wakeSolver.py:345-369, 449-529)."""
+    def _wp_index(self, nsaved):
+        """s and the raw time index it(m, k) exactly as calc_long_WP_3d / calc_long_WP
+        evaluate them (wakis/wakeSolver.py:345-369, 449-529), the z trim and nt."""
         nt = len(self.t)
         dt = self.t[2] - self.t[1]
         ti = self.ti
@@ -112,10 +112,6 @@ class WakeSolver:
         zmin = np.min(self.zf)
         zz = slice(self.skip_cells, -self.skip_cells) if self.skip_cells != 0 else np.s_[:]
         z = self.zf[zz]
-        nz = len(z)
-        if longitudinal and nz != Nz:
-            raise ValueError(f"could not broadcast input array from shape ({Nz},) into shape ({nz},): "
-                             f"compute_plane='longitudinal' needs skip_cells=0")
         if self.wakelength is not None:
             wakelength = self.wakelength
         else:
@@ -124,12 +120,18 @@ class WakeSolver:
         s = np.arange(-self.ti * self.v, wakelength, dt * self.v)
         nt = min(nt, nsaved)
         ts = (z[None, :] + s[:, None]) / self.v - zmin / self.v - self.t[0] + ti
-        q = ts / dt
-        it = np.trunc(q).astype(np.int64)
+        it = np.trunc(ts / dt).astype(np.int64)
+        return s, it, zz, len(z), nt
+
+    def _tap_index(self, nsaved, longitudinal, Nz):
+        """s and it(m, k) of the device taps of a live run."""
+        s, it, zz, nz, nt = self._wp_index(nsaved)
+        if longitudinal and nz != Nz:
+            raise ValueError(f"could not broadcast input array from shape ({Nz},) into shape ({nz},): "
+                             f"compute_plane='longitudinal' needs skip_cells=0")
         valid = it < nt
         if np.any(valid & (it < 0)):
             raise NotImplementedError("negative time index in the wake integral (a tap before t=0)")
-        self._s_pending = s
         kskip = self.skip_cells if self.skip_cells != 0 else 0
         return s, it, valid, kskip, nz, nt
 
@@ -193,16 +195,64 @@ class WakeSolver:
             self.calc_long_Z()
         self.log("Calculation terminated in %ds" % (time.time() - t0))
 
-    def _require_run(self):
-        if self._run is None:
-            raise RuntimeError("no device wake run attached: call solver.wakesolve(...) on a wakis_gb300 "
-                               "SolverFIT3D (reading an Ez.h5 file written elsewhere needs h5py)")
+    def _history_wp(self, longitudinal, Ezt=None):
+        """The wake integral of an Ez file: without a live run, calc_long_WP and
+        calc_long_WP_3d read the per-step slabs of ``Ez_file`` (HDF5, or the .npz archive
+        with the same keys) and evaluate the integral on the device in the reference's
+        operation order, so s and WP / WP_3d equal the reference's bit for bit
+        (wakis/wakeSolver.py:333-413, 446-540).  Slab lines follow the reference: the 1-D
+        slab itself, or Ez[sh0//2 + 1, sh1//2 + 1, zz] for calc_long_WP on 3-D slabs,
+        Ez[sh0//2 + i, sh1//2 + j, zz] for the 3x3 lines of calc_long_WP_3d.  The file is
+        closed afterwards, as the reference closes it."""
+        if Ezt is not None:
+            self.Ezt = Ezt
+            if self.Ez_hf is None:
+                # the reference keeps Ezt and then assembles it again from the unopened file
+                raise AttributeError("'NoneType' object has no attribute 'keys'")
+        elif self.Ez_hf is None:
+            self.read_Ez()
+        hf = self.Ez_hf
+        keys = sorted(k for k in hf.keys() if isinstance(k, str) and k.startswith("#"))
+        if not keys:
+            raise IndexError("list index out of range")
+        s, it, zz, nz, nt = self._wp_index(len(keys))
+        ofs = [(1, 1)] if longitudinal else [(i, j) for i in (-1, 0, 1) for j in (-1, 0, 1)]
+        ezt = np.zeros((len(ofs), nz, nt))
+        ndim = np.ndim(hf[keys[0]])
+        for n in range(nt):
+            E = np.asarray(hf[keys[n]])
+            if longitudinal and ndim == 1:
+                ezt[0, :, n] = E
+            elif longitudinal and ndim != 3:
+                continue  # the reference leaves Ezt at zero for other slab shapes
+            else:
+                for li, (i, j) in enumerate(ofs):
+                    ezt[li, :, n] = E[E.shape[0] // 2 + i, E.shape[1] // 2 + j, zz]
+        valid = it < nt
+        itw = np.where(it < 0, it + nt, it)
+        if np.any(valid & (itw < 0)):
+            bad = int(it[valid & (itw < 0)][0])
+            raise IndexError(f"index {bad} is out of bounds for axis 1 with size {nt}")
+        table = np.ascontiguousarray(np.where(valid, itw, -1).T, dtype=np.int32)  # (nz, ns)
+        dz = np.asarray(self.dz, dtype=np.float64)[:nz]
+        if len(ofs) == 9:
+            dxf, dyf = np.diff(self.xf), np.diff(self.yf)
+            wp3d, wpx, wpy = nat.wake_history(ezt, table, dz, self.q * 1e12, s[2] - s[1], dxf[0] + dxf[1],
+                                              dyf[0] + dyf[1])
+        else:
+            wp3d, wpx, wpy = nat.wake_history(ezt, table, dz, self.q * 1e12)
+        hf.close()
+        self.Ez_hf = None
+        return s, wp3d, wpx, wpy, ezt
 
     def calc_long_WP(self, Ezt=None, **kwargs):
         for key, val in kwargs.items():
             setattr(self, key, val)
-        self._require_run()
-        s, wp3d, _, _ = self._finalize_device()
+        if self._run is not None:
+            s, wp3d, _, _ = self._finalize_device()
+        else:
+            s, wp3d, _, _, ezt = self._history_wp(True, Ezt)
+            self.Ezt = ezt[0]
         self.s = s
         self.WP = wp3d[0]
         if self.save:
@@ -211,8 +261,10 @@ class WakeSolver:
     def calc_long_WP_3d(self, **kwargs):
         for key, val in kwargs.items():
             setattr(self, key, val)
-        self._require_run()
-        s, wp3d, wpx, wpy = self._finalize_device()
+        if self._run is not None:
+            s, wp3d, wpx, wpy = self._finalize_device()
+        else:
+            s, wp3d, wpx, wpy, _ = self._history_wp(False)
         self.s = s
         self.WP_3d = wp3d.reshape(3, 3, len(s))
         self.WP = self.WP_3d[1, 1, :]
@@ -226,7 +278,6 @@ class WakeSolver:
         for key, val in kwargs.items():
             setattr(self, key, val)
         if getattr(self, "_wpxy", None) is None:
-            self._require_run()
             self.calc_long_WP_3d()
         self.WPx, self.WPy = self._wpxy
         if self.save:
