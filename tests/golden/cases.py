@@ -147,6 +147,18 @@ CASES = {
         source=dict(type="PlaneWave", xs=(0, 6), ys=(0, 6), zs=0, beta=1.0, amplitude=100.0,
                     f_nodes=15, nodes=7, phase=np.pi / 2),
         dt_override="1/f/200", Nt=150),
+    # test_003 layout at reduced size: plane wave (f = 15 nodes over the domain, source on
+    # the interior cells of plane 1, default dt) onto a dielectric sphere eps_r = 10,
+    # periodic x/y, PEC z-lo, PML z-hi
+    "planewave_sphere_f32": dict(
+        kind="emsolve", dtype="float32",
+        grid=dict(xmin=-6 * MM, xmax=6 * MM, ymin=-6 * MM, ymax=6 * MM, zmin=-15 * MM, zmax=15 * MM,
+                  Nx=12, Ny=12, Nz=24),
+        solids=[("Sphere", "sphere", {"R": 5 * MM}, [10.0, 1.0])], bg=[1.0, 1.0],
+        bc_low=["periodic", "periodic", "pec"], bc_high=["periodic", "periodic", "pml"], n_pml=10, cfln=0.5,
+        source=dict(type="PlaneWave", xs=(1, 11), ys=(1, 11), zs=1, beta=1.0, amplitude=1.0,
+                    f_nodes=15, nodes=None, phase=0),
+        Nt=90),
     # config-2 layout at reduced size: PML on all faces, dielectric sphere, wave packet
     "wavepacket_f64": dict(
         kind="emsolve", dtype="float64",

@@ -85,3 +85,58 @@ def close(a, b, f64):
     if not np.any(b):
         return not np.any(a)
     return rel_l2(a, b) < (1e-12 if f64 else 1e-5)
+
+
+@pytest.mark.parametrize("name", FUSED_CASES)
+def test_coded_coefficients_equal_dense(name, tmp_path, monkeypatch):
+    """The fused step with coded coefficients (a 16-bit code per cell into a table of the
+    exact (ch, ce, cl) triples) gives the dense fused step's results bit for bit."""
+    monkeypatch.setenv("WAKIS_GB300_KERNELS", "fused")
+    monkeypatch.setenv("WAKIS_GB300_CODES", "1")
+    coded = run_case(name, tmpdir=tmp_path)
+    monkeypatch.setenv("WAKIS_GB300_CODES", "0")
+    dense = run_case(name, tmpdir=tmp_path)
+    for k, v in dense.items():
+        np.testing.assert_array_equal(np.asarray(coded[k]), np.asarray(v), err_msg=f"{name}:{k}")
+
+
+def _random_field_solver(x, y, z, dtype, codes, bcs=(["pec", "pmc", "pec"], ["pml", "pec", "pmc"])):
+    import wakis_gb300 as wg
+    blk = lambda X, Y, Z: (np.abs(X) < 0.4) & (Z > 0.3) & (Z < 1.1)
+    grid = wg.GridFIT3D(x=x, y=y, z=z, stl_solids={"blk": blk}, stl_materials={"blk": [2.0, 1.0, 50.0]}, verbose=0)
+    s = wg.SolverFIT3D(grid, cfln=0.5, bc_low=bcs[0], bc_high=bcs[1], use_stl=True, bg=[1.0, 1.0], dtype=dtype,
+                       n_pml=4, verbose=0)
+    s.kernels = "fused"
+    s.coefficient_codes = codes
+    rng = np.random.default_rng(9)
+    s.E.fromarray(rng.standard_normal((s.Nx, s.Ny, s.Nz, 3)).astype(dtype))
+    s.H.fromarray(rng.standard_normal((s.Nx, s.Ny, s.Nz, 3)).astype(dtype))
+    return s
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_coded_step_random_fields(dtype):
+    """Random fields on a 16 x 12 x 40 grid with lossy blocks, PML and PMC faces: coded and
+    dense fused device loops agree bit for bit, and the grid is coded."""
+    x = np.linspace(-1, 1, 17)
+    y = np.linspace(-0.8, 0.7, 13)
+    z = np.linspace(-2, 2, 41)
+    out = {}
+    for codes in (True, False):
+        s = _random_field_solver(x, y, z, dtype, codes)
+        s.emsolve(33)
+        out[codes] = (s.E.numpy(), s.H.numpy(), s.J.numpy(), s.coefficient_code_count)
+    assert out[True][3] > 0 and out[False][3] == 0
+    for a, b, k in zip(out[True][:3], out[False][:3], "EHJ"):
+        np.testing.assert_array_equal(a, b, err_msg=k)
+
+
+def test_grid_with_too_many_coefficient_triples_stays_dense():
+    """48^3 cells with random spacing along every axis have more than 65535 distinct
+    coefficient triples: the context stays dense (code count 0) and still steps."""
+    rng = np.random.default_rng(4)
+    ax = lambda n: np.concatenate([[0.0], np.cumsum(0.5 + rng.random(n))])
+    s = _random_field_solver(ax(48) - 24, ax(48) - 24, ax(48) - 24, np.float32, True)
+    s.emsolve(4)
+    assert s.coefficient_code_count == 0
+    assert np.isfinite(s.E.numpy()).all()

@@ -87,6 +87,7 @@ _SIGS = {
     "fit_set_kernel_variant": (_P, C.c_int32),
     "fit_time_fused": (_P, C.c_int32, _D),
     "fit_set_fused_shape": (_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32),
+    "fit_set_coeff_codes": (_P, C.c_int32, C.POINTER(C.c_int32)),
     "fit_monitor_update": (_P, C.c_int32, C.c_int64, C.c_int32, _D, _P, C.c_int32, _P),
     "fit_set_monitor": (_P, C.c_int32, _D, C.c_int64, C.c_int64, _P, C.c_int32),
     "fit_set_ez_record": (_P, _P, C.c_int32, _I32, _I32, C.c_int64, C.c_int64),

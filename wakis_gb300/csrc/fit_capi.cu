@@ -88,6 +88,9 @@ struct FitCtx {
     void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
     int fused_vec = 4, fused_rows = 8, fused_zseg = 1, fused_ctas = 2;  // tile shape of the fused step
     bool graph_fused = false;  // the cached graph holds fused steps
+    unsigned short* d_code = nullptr;  // coded coefficients: one code per cell (nullptr: dense)
+    void* d_tab = nullptr;             // [code][ch, ce, cl][x, y, z, pad] in the field dtype
+    int ncodes = 0;
     RecordArgs rec{};           // Ez line history of recorded steps (nlines = 0: off)
     MonitorArgs mon{};          // field monitor epilogue of device-loop steps (nf = 0: off)
     double2* d_mon_phases = nullptr;
@@ -209,6 +212,17 @@ void invalidate(FitCtx* c) {
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
+}
+
+// back to dense coefficients (the cached graph may hold coded launches)
+void drop_codes(FitCtx* c) {
+    if (!c->d_code) return;
+    invalidate(c);
+    dfree(c->d_code, c->own);
+    dfree(c->d_tab, c->own);
+    c->d_code = nullptr;
+    c->d_tab = nullptr;
+    c->ncodes = 0;
 }
 
 int launches_per_step(const FitCtx* c) {
@@ -353,7 +367,9 @@ bool fused_ok(const FitCtx* c, int mode) {
     return c->fused && c->E2 && c->H2 && mode != 2 && !c->plane.active && !c->abc_axes && pick_vec(c) >= 2;
 }
 
-template <typename T, int VEC, int FY, int MB>
+// DENSE: also instantiate the dense-coefficient kernels (the coded kernels need fewer
+// registers, so the higher CTA counts per SM exist for them only)
+template <typename T, int VEC, int FY, int MB, bool DENSE = true>
 void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
     constexpr int FX = 32 * VEC;
     const T* Ein = static_cast<const T*>(forward ? c->E : c->E2);
@@ -368,22 +384,42 @@ void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, c
     const T* ce = static_cast<const T*>(c->ce);
     const T* cl = static_cast<const T*>(c->cl);
     T* J = static_cast<T*>(c->J);
-    if (mode == 1)
-        k_step_fused<T, VEC, FY, MB, 1><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond,
-                                                                  c->g, metric<T>(c), beam, st, zlen);
-    else
-        k_step_fused<T, VEC, FY, MB, 0><<<grid, block, 0, c->own>>>(Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond,
-                                                                  c->g, metric<T>(c), beam, st, zlen);
+    const unsigned short* code = c->d_code;
+    const T* tab = static_cast<const T*>(c->d_tab);
+    if (mode == 1 && code) {
+        k_step_fused<T, VEC, FY, MB, 1, true><<<grid, block, 0, c->own>>>(
+            Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g, metric<T>(c), beam, st, zlen, code, tab);
+    } else if (code) {
+        k_step_fused<T, VEC, FY, MB, 0, true><<<grid, block, 0, c->own>>>(
+            Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g, metric<T>(c), beam, st, zlen, code, tab);
+    } else if constexpr (DENSE) {
+        if (mode == 1)
+            k_step_fused<T, VEC, FY, MB, 1, false><<<grid, block, 0, c->own>>>(
+                Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g, metric<T>(c), beam, st, zlen, nullptr,
+                nullptr);
+        else
+            k_step_fused<T, VEC, FY, MB, 0, false><<<grid, block, 0, c->own>>>(
+                Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g, metric<T>(c), beam, st, zlen, nullptr,
+                nullptr);
+    }
     count(c);
 }
 
 // the fused step in the context's tile shape: fused_vec cells per thread, fused_rows rows,
-// register budget for fused_ctas CTAs per SM (8 rows: 2; 4 rows: 3 or 4)
+// register budget for fused_ctas CTAs per SM (8 rows: 2, coded also 3; 4 rows: 3 or 4,
+// coded also 5 or 6).  A coded-only budget on a dense context runs the nearest dense one.
 template <typename T, int VEC>
 void launch_fused_vec(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
-    if (c->fused_rows == 8)
+    const bool coded = c->d_code != nullptr;
+    if (c->fused_rows == 8 && c->fused_ctas == 3 && coded)
+        launch_fused_shape<T, VEC, 8, 3, false>(c, mode, st, forward, beam);
+    else if (c->fused_rows == 8)
         launch_fused_shape<T, VEC, 8, 2>(c, mode, st, forward, beam);
-    else if (c->fused_ctas == 4)
+    else if (c->fused_ctas == 6 && coded)
+        launch_fused_shape<T, VEC, 4, 6, false>(c, mode, st, forward, beam);
+    else if (c->fused_ctas == 5 && coded)
+        launch_fused_shape<T, VEC, 4, 5, false>(c, mode, st, forward, beam);
+    else if (c->fused_ctas >= 4)
         launch_fused_shape<T, VEC, 4, 4>(c, mode, st, forward, beam);
     else
         launch_fused_shape<T, VEC, 4, 3>(c, mode, st, forward, beam);
@@ -443,6 +479,68 @@ int check_ready(FitCtx* c) {
     if (!c->metrics_set) return fail(c, FIT_ERR_STATE, "fit_set_metrics has not been called");
     if (!c->coeffs_set) return fail(c, FIT_ERR_STATE, "fit_set_coeffs has not been called");
     if (!c->E || !c->H || !c->J) return fail(c, FIT_ERR_STATE, "field pointers are not set");
+    return FIT_OK;
+}
+
+// one pass of the code build in the field dtype (kernels k_code_*)
+template <typename T>
+int build_codes_t(FitCtx* c, int32_t* ncodes) {
+    const long long N = c->g.N;
+    unsigned long long* keys = nullptr;
+    T* vals = nullptr;
+    int* slot_code = nullptr;
+    int* status = nullptr;
+    void* tab = nullptr;
+    unsigned short* code = nullptr;
+    auto release = [&](bool keep) {
+        dfree(keys, c->own);
+        dfree(vals, c->own);
+        dfree(slot_code, c->own);
+        dfree(status, c->own);
+        if (!keep) {
+            dfree(tab, c->own);
+            dfree(code, c->own);
+        }
+    };
+    int rc = dev_alloc(c, (void**)&keys, kCodeSlots * sizeof(unsigned long long));
+    if (!rc) rc = dev_alloc(c, (void**)&vals, (size_t)kCodeSlots * 9 * sizeof(T));
+    if (!rc) rc = dev_alloc(c, (void**)&slot_code, kCodeSlots * sizeof(int));
+    if (!rc) rc = dev_alloc(c, (void**)&status, 4 * sizeof(int));
+    if (!rc) rc = dev_alloc(c, &tab, (size_t)kMaxCodes * 12 * sizeof(T));
+    if (!rc) rc = dev_alloc(c, (void**)&code, (size_t)N * sizeof(unsigned short));
+    if (rc) {
+        release(false);
+        return rc;
+    }
+    cudaError_t e = cudaMemsetAsync(keys, 0, kCodeSlots * sizeof(unsigned long long), c->own);
+    if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, 4 * sizeof(int), c->own);
+    const T* ch = static_cast<const T*>(c->ch);
+    const T* ce = static_cast<const T*>(c->ce);
+    const T* cl = static_cast<const T*>(c->cl);
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>((N + 255) / 256, 8LL * c->nsm));
+    if (e == cudaSuccess) {
+        k_code_insert<T><<<blocks, 256, 0, c->own>>>(ch, ce, cl, N, keys, vals, status);
+        k_code_number<T><<<1, 1024, 0, c->own>>>(keys, vals, slot_code, static_cast<T*>(tab), status);
+        k_code_assign<T><<<blocks, 256, 0, c->own>>>(ch, ce, cl, N, keys, slot_code, static_cast<const T*>(tab),
+                                                     code, status);
+        count(c, 3);
+        e = cudaGetLastError();
+    }
+    int st[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st, status, sizeof(st), cudaMemcpyDeviceToHost, c->own);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->own);
+    if (e != cudaSuccess) {
+        release(false);
+        return fail(c, FIT_ERR_CUDA, "coefficient codes: %s", cudaGetErrorString(e));
+    }
+    const bool ok = st[0] == 0 && st[1] <= kMaxCodes && st[2] == 0;
+    release(ok);
+    *ncodes = ok ? st[1] : 0;
+    if (ok) {
+        c->d_code = code;
+        c->d_tab = tab;
+        c->ncodes = st[1];
+    }
     return FIT_OK;
 }
 
@@ -546,7 +644,9 @@ int fit_ctx_destroy(FitCtx* c) {
         dfree(c->tL_T[a], c->own);
         dfree(c->L_T[a], c->own);
     }
-    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg, c->E2, c->H2, (void*)c->d_mon_phases}) dfree(p, c->own);
+    for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg, c->E2, c->H2, (void*)c->d_mon_phases, (void*)c->d_code,
+                    c->d_tab})
+        dfree(p, c->own);
     for (void* p : {(void*)c->d_beam_z, (void*)c->d_beam_dtieps, (void*)c->d_vt_table, (void*)c->d_prof,
                     (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
                     (void*)c->d_em, (void*)c->d_ek0, (void*)c->d_ecnt, (void*)c->d_dz, (void*)c->d_acc,
@@ -643,6 +743,7 @@ int fit_set_coeffs(FitCtx* c, double dt, const double* ieps, const double* imu, 
     if (!c->metrics_set) return fail(c, FIT_ERR_STATE, "fit_set_metrics must precede fit_set_coeffs");
     int rc = enter(c);
     if (rc) return rc;
+    drop_codes(c);  // the codes describe the coefficients being replaced
     CoeffArgs a{};
     for (int i = 0; i < 3; ++i) {
         a.L[i] = c->dL[i];
@@ -1224,12 +1325,35 @@ int fit_set_kernel_variant(FitCtx* c, int32_t variant) {
     return FIT_OK;
 }
 
+int fit_set_coeff_codes(FitCtx* c, int32_t enable, int32_t* ncodes) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    int32_t dummy = 0;
+    if (!ncodes) ncodes = &dummy;
+    *ncodes = 0;
+    if (!enable) {
+        drop_codes(c);
+        return FIT_OK;
+    }
+    if (!c->coeffs_set || !c->ch || !c->ce) return fail(c, FIT_ERR_STATE, "fit_set_coeffs must precede the codes");
+    if (c->d_code) {
+        *ncodes = c->ncodes;
+        return FIT_OK;
+    }
+    int rc = enter(c);
+    if (rc) return rc;
+    invalidate(c);
+    rc = c->dtype == FIT_F64 ? build_codes_t<double>(c, ncodes) : build_codes_t<float>(c, ncodes);
+    if (rc) return rc;
+    return leave(c);
+}
+
 int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg, int32_t ctas) {
     if (!c) return FIT_ERR_ARG;
     if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     const bool vec_ok = (vec == 2 && c->g.nx % 2 == 0) || (vec == 4 && c->dtype == FIT_F32 && c->g.nx % 4 == 0);
     if (ctas == 0) ctas = rows == 8 ? 2 : 3;
-    const bool ctas_ok = (rows == 8 && ctas == 2) || (rows == 4 && (ctas == 3 || ctas == 4));
+    const bool ctas_ok = (rows == 8 && (ctas == 2 || ctas == 3)) || (rows == 4 && ctas >= 3 && ctas <= 6);
     if (!vec_ok || !ctas_ok || zseg < 1 || zseg > c->g.nz)
         return fail(c, FIT_ERR_ARG, "bad fused tile shape (vec %d, rows %d, z ranges %d, CTAs/SM %d)", vec, rows, zseg,
                     ctas);

@@ -204,6 +204,59 @@ __device__ __forceinline__ void zero_v(T (&r)[VEC]) {
     for (int e = 0; e < VEC; ++e) r[e] = T(0);
 }
 
+// ---------------------------------------------------------------- coded coefficients
+// A grid has few distinct per-cell coefficient triples (ch, ce, cl): uniform spacing,
+// a handful of materials, graded PML planes.  A coded context stores one 16-bit code
+// per cell and a table tab[code][group][4] (group 0 ch, 1 ce, 2 cl; x, y, z, pad) that
+// holds the exact values of the dense arrays, so a coded step gives the dense step's
+// results bit for bit while reading 2 bytes instead of 9 words per cell.
+template <int VEC>
+__device__ __forceinline__ void ld_codes(unsigned (&c)[VEC], const unsigned short* __restrict__ p) {
+    if constexpr (VEC == 4) {
+        const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+        c[0] = t.x & 0xffffu; c[1] = t.x >> 16; c[2] = t.y & 0xffffu; c[3] = t.y >> 16;
+    } else if constexpr (VEC == 2) {
+        const unsigned t = __ldg(reinterpret_cast<const unsigned*>(p));
+        c[0] = t & 0xffffu; c[1] = t >> 16;
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) c[e] = __ldg(p + e);
+    }
+}
+template <typename T>
+__device__ __forceinline__ void tab_get(const T* __restrict__ tab, unsigned code, int grp, T& x, T& y, T& z) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(tab) + 3 * code + grp);
+        x = t.x; y = t.y; z = t.z;
+    } else {
+        const double2* q = reinterpret_cast<const double2*>(tab) + 2 * (3 * code + grp);
+        const double2 a = __ldg(q), b = __ldg(q + 1);
+        x = a.x; y = a.y; z = b.x;
+    }
+}
+// the VEC cells of a thread mostly share one code (material boundaries are rare): one
+// table read then serves all of them
+template <typename T, int VEC>
+__device__ __forceinline__ void tab_get_v(const T* __restrict__ tab, const unsigned (&c)[VEC], int grp, T (&x)[VEC],
+                                          T (&y)[VEC], T (&z)[VEC]) {
+    bool same = true;
+#pragma unroll
+    for (int e = 1; e < VEC; ++e) same = same && c[e] == c[0];
+    if (same) {
+        T a, b, d;
+        tab_get<T>(tab, c[0], grp, a, b, d);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            x[e] = a;
+            y[e] = b;
+            z[e] = d;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) tab_get<T>(tab, c[e], grp, x[e], y[e], z[e]);
+    }
+}
+
 // ---------------------------------------------------------------- beam line current
 // sources.Beam.update (wakis/sources.py:98-110), evaluated in FP64 with the reference's
 // operation order:  J = ((q*v)*profile)/dx/dy,
@@ -450,10 +503,12 @@ __device__ __forceinline__ void cell_of(long long n, const Geom& g, int& i0, int
 // whose Nx is not a multiple of the 16-byte vector width and for the explicit-J pass.
 // New H of the VEC cells starting at component-local flat index n (cell (i0, j, k)),
 // from E and the old H: the values land in hx, hy, hz; nothing is stored.
-template <typename T, int VEC>
+template <typename T, int VEC, bool CODED = false>
 __device__ __forceinline__ void hpass_eval(const T* __restrict__ E, const T* H, const T* __restrict__ ch,
                                            const Geom& g, const Metric<T>& mt, long long n, int i0, int j, int k,
-                                           T (&hx)[VEC], T (&hy)[VEC], T (&hz)[VEC]) {
+                                           T (&hx)[VEC], T (&hy)[VEC], T (&hz)[VEC],
+                                           const unsigned short* __restrict__ code = nullptr,
+                                           const T* __restrict__ tab = nullptr, const unsigned* pre = nullptr) {
     const T* Ex = E;
     const T* Ey = E + g.N;
     const T* Ez = E + 2 * g.N;
@@ -487,9 +542,20 @@ __device__ __forceinline__ void hpass_eval(const T* __restrict__ E, const T* H, 
     ld_v<T, VEC>(hx, H + n);
     ld_v<T, VEC>(hy, H + g.N + n);
     ld_v<T, VEC>(hz, H + 2 * g.N + n);
-    ldg_v<T, VEC>(cx, ch + n);
-    ldg_v<T, VEC>(cy, ch + g.N + n);
-    ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
+    if constexpr (CODED) {
+        unsigned cd[VEC];
+        if (pre) {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) cd[e] = pre[e];
+        } else {
+            ld_codes<VEC>(cd, code + n);
+        }
+        tab_get_v<T, VEC>(tab, cd, 0, cx, cy, cz);
+    } else {
+        ldg_v<T, VEC>(cx, ch + n);
+        ldg_v<T, VEC>(cy, ch + g.N + n);
+        ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
+    }
     hpass_cells<T, VEC>(ex, ey, ez, exy, ezy, exz, eyz, eyx, ezx, hx, hy, hz, cx, cy, cz, i0, j, k, g, mt);
 }
 
@@ -683,12 +749,14 @@ struct FusedShared {
 
 // The march of one tile column (bx, by) through planes k0 .. k1-1 (all threads of the
 // CTA call it; the plane buffers in sm are free on entry).
-template <typename T, int VEC, int FY, int MODE>
+template <typename T, int VEC, int FY, int MODE, bool CODED = false>
 __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout,
                                             T* __restrict__ Hout, const T* __restrict__ ch, const T* __restrict__ ce,
                                             const T* __restrict__ cl, T* __restrict__ J, int use_cond, const Geom& g,
                                             const Metric<T>& mt, const BeamArgs& b, const StepArgs& st, int bx, int by,
-                                            int k0, int k1, FusedShared<T, VEC, FY>& sm) {
+                                            int k0, int k1, FusedShared<T, VEC, FY>& sm,
+                                            const unsigned short* __restrict__ code = nullptr,
+                                            const T* __restrict__ tab = nullptr) {
     constexpr int FX = 32 * VEC;
     const int lane = threadIdx.x, ty = threadIdx.y;
     const bool halo = ty == FY;  // the halo warp
@@ -701,7 +769,7 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
     if (k0 > 0 && on && !halo) {  // new H of plane k0-1 (the plane below the range) for the tile
         T hx[VEC], hy[VEC], hz[VEC];
         const long long n = (long long)i0 + g.sy * j + g.sz * (k0 - 1);
-        hpass_eval<T, VEC>(Ein, Hin, ch, g, mt, n, i0, j, k0 - 1, hx, hy, hz);
+        hpass_eval<T, VEC, CODED>(Ein, Hin, ch, g, mt, n, i0, j, k0 - 1, hx, hy, hz, code, tab);
         const int bp = (k0 - 1) % 3;
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
@@ -715,6 +783,7 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
         const long long n = (long long)i0 + g.sy * j + g.sz * k;
         T hx[VEC], hy[VEC], hz[VEC];
         T kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
+        unsigned cd[VEC];
         if constexpr (MODE != 1) {
             zero_v<T, VEC>(lx);
             zero_v<T, VEC>(ly);
@@ -727,7 +796,7 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
                 if (m >= 0) {
                     int mi, mj, mk;
                     cell_of(m, g, mi, mj, mk);
-                    hpass_eval<T, VEC>(Ein, Hin, ch, g, mt, m, mi, mj, mk, ax, ay, az);
+                    hpass_eval<T, VEC, CODED>(Ein, Hin, ch, g, mt, m, mi, mj, mk, ax, ay, az, code, tab);
                 } else {
                     zero_v<T, VEC>(ax);
                     zero_v<T, VEC>(az);
@@ -746,7 +815,7 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
                 if (m >= 0) {
                     int mi, mj, mk;
                     cell_of(m, g, mi, mj, mk);
-                    hpass_eval<T, 1>(Ein, Hin, ch, g, mt, m, mi, mj, mk, ax, ay, az);
+                    hpass_eval<T, 1, CODED>(Ein, Hin, ch, g, mt, m, mi, mj, mk, ax, ay, az, code, tab);
                 } else {
                     ay[0] = T(0);
                     az[0] = T(0);
@@ -756,16 +825,21 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
             }
         } else if (on) {
             // the E update's coefficients do not depend on the new H: load them first so
-            // their latency overlaps the H update and the barrier
-            ldg_v<T, VEC>(kx, ce + n);
-            ldg_v<T, VEC>(ky, ce + g.N + n);
-            ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
-            if constexpr (MODE == 1) {
-                ldg_v<T, VEC>(lx, cl + n);
-                ldg_v<T, VEC>(ly, cl + g.N + n);
-                ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+            // their latency overlaps the H update and the barrier (coded: the codes; the
+            // table entries are L1 hits, read after the barrier)
+            if constexpr (CODED) {
+                ld_codes<VEC>(cd, code + n);
+            } else {
+                ldg_v<T, VEC>(kx, ce + n);
+                ldg_v<T, VEC>(ky, ce + g.N + n);
+                ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+                if constexpr (MODE == 1) {
+                    ldg_v<T, VEC>(lx, cl + n);
+                    ldg_v<T, VEC>(ly, cl + g.N + n);
+                    ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+                }
             }
-            hpass_eval<T, VEC>(Ein, Hin, ch, g, mt, n, i0, j, k, hx, hy, hz);
+            hpass_eval<T, VEC, CODED>(Ein, Hin, ch, g, mt, n, i0, j, k, hx, hy, hz, code, tab, cd);
             st_v<T, VEC>(Hout + n, hx);
             st_v<T, VEC>(Hout + g.N + n, hy);
             st_v<T, VEC>(Hout + 2 * g.N + n, hz);
@@ -798,6 +872,10 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
             const T hzx = lane > 0 ? sm.h[bc][2][ty + 1][xo - 1] : sm.hx1[bc][1][ty + 1];
             T cur[3][VEC];
             epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
+            if constexpr (CODED) {
+                tab_get_v<T, VEC>(tab, cd, 1, kx, ky, kz);
+                if constexpr (MODE == 1) tab_get_v<T, VEC>(tab, cd, 2, lx, ly, lz);
+            }
             T ex[VEC], ey[VEC], ez[VEC];
             ldg_v<T, VEC>(ex, Ein + n);
             ldg_v<T, VEC>(ey, Ein + g.N + n);
@@ -810,16 +888,18 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
     }
 }
 
-// MB: CTAs per SM the register budget is sized for (the launch bound)
-template <typename T, int VEC, int FY, int MB, int MODE>
+// MB: CTAs per SM the register budget is sized for (the launch bound).  CODED: the
+// coefficients come from code/tab instead of ch/ce/cl.
+template <typename T, int VEC, int FY, int MB, int MODE, bool CODED>
 __global__ void __launch_bounds__(32 * (FY + 1), MB)
     k_step_fused(const T* __restrict__ Ein, const T* __restrict__ Hin, T* __restrict__ Eout, T* __restrict__ Hout,
                  const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl, T* __restrict__ J,
-                 int use_cond, Geom g, Metric<T> mt, BeamArgs b, StepArgs st, int zlen) {
+                 int use_cond, Geom g, Metric<T> mt, BeamArgs b, StepArgs st, int zlen,
+                 const unsigned short* __restrict__ code, const T* __restrict__ tab) {
     __shared__ FusedShared<T, VEC, FY> sm;
     const int k0 = blockIdx.z * zlen;
-    fused_march<T, VEC, FY, MODE>(Ein, Hin, Eout, Hout, ch, ce, cl, J, use_cond, g, mt, b, st, blockIdx.x, blockIdx.y,
-                                  k0, min(g.nz, k0 + zlen), sm);
+    fused_march<T, VEC, FY, MODE, CODED>(Ein, Hin, Eout, Hout, ch, ce, cl, J, use_cond, g, mt, b, st, blockIdx.x,
+                                         blockIdx.y, k0, min(g.nz, k0 + zlen), sm, code, tab);
 }
 
 // ---------------------------------------------------------------- staged kernels
@@ -1185,6 +1265,164 @@ __global__ void k_build_coeffs(const double* __restrict__ ieps, const double* __
 }
 
 // ---------------------------------------------------------------- small kernels
+// ---------------------------------------------------------------- coefficient code build
+// Three passes over the dense coefficients of a context: (1) insert every cell's
+// (ch, ce, cl) triple, keyed by a 64-bit hash of its bits, into an open-addressing table
+// (one insert per distinct key and warp, others find their key already present);
+// (2) number the occupied slots in slot order and copy their triples into the code
+// table; (3) give every cell the code of its key and compare its triple with the code
+// table bit for bit.  Any mismatch (a hash collision), a full table or more than
+// kMaxCodes distinct triples leaves the context dense.  No pass waits on another thread.
+constexpr int kCodeSlots = 1 << 17;
+constexpr int kMaxCodes = 65535;
+constexpr int kCodeProbes = 4096;  // probe bound; the table is at most half full while codes fit
+
+template <typename T>
+__device__ __forceinline__ unsigned long long word_bits(T v) {
+    if constexpr (sizeof(T) == 4) return (unsigned long long)__float_as_uint(v);
+    else return (unsigned long long)__double_as_longlong(v);
+}
+
+template <typename T>
+__device__ __forceinline__ void coef_triple(const T* __restrict__ ch, const T* __restrict__ ce,
+                                            const T* __restrict__ cl, long long N, long long n, T (&v)[9]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = ch[c * N + n];
+        v[3 + c] = ce[c * N + n];
+        v[6 + c] = cl ? cl[c * N + n] : T(0);
+    }
+}
+
+// FNV-1a over the nine words, then the 64-bit finaliser of MurmurHash3; 0 marks an
+// empty slot and is never returned
+template <typename T>
+__device__ __forceinline__ unsigned long long triple_hash(const T (&v)[9]) {
+    unsigned long long h = 0xcbf29ce484222325ULL;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) h = (h ^ word_bits(v[i])) * 0x100000001b3ULL;
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdULL;
+    h ^= h >> 33;
+    h *= 0xc4ceb9fe1a85ec53ULL;
+    h ^= h >> 33;
+    return h ? h : 1ULL;
+}
+
+// status: [0] too many triples (more than kMaxCodes inserted, or a probe bound hit),
+// [1] number of codes, [2] cells whose triple differs from its code's, [3] keys inserted
+template <typename T>
+__global__ void k_code_insert(const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl,
+                              long long N, unsigned long long* keys, T* __restrict__ vals, int* status) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // the trip count and the stop decision are uniform across each warp, so the
+    // warp-wide match below is legal
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < N; base += stride) {
+        int stop = 0;
+        if ((threadIdx.x & 31) == 0) stop = *(volatile int*)&status[0];
+        if (__shfl_sync(0xffffffffu, stop, 0)) break;
+        const long long n = base + threadIdx.x;
+        const bool valid = n < N;
+        T v[9];
+        unsigned long long h = 0;
+        if (valid) {
+            coef_triple<T>(ch, ce, cl, N, n, v);
+            h = triple_hash<T>(v);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, h);
+        if (!valid || (int)(__ffs(peers) - 1) != (int)(threadIdx.x & 31)) continue;
+        unsigned slot = (unsigned)h & (kCodeSlots - 1);
+        int p = 0;
+        for (; p < kCodeProbes; ++p) {
+            const unsigned long long cur = keys[slot];
+            if (cur == h) break;
+            if (cur == 0) {
+                const unsigned long long old = atomicCAS(&keys[slot], 0ULL, h);
+                if (old == 0) {
+#pragma unroll
+                    for (int i = 0; i < 9; ++i) vals[(long long)slot * 9 + i] = v[i];
+                    if (atomicAdd(&status[3], 1) >= kMaxCodes) atomicExch(&status[0], 1);
+                    break;
+                }
+                if (old == h) break;
+            }
+            slot = (slot + 1) & (kCodeSlots - 1);
+        }
+        if (p == kCodeProbes) atomicExch(&status[0], 1);
+    }
+}
+
+// one block of 1024 threads, kCodeSlots / 1024 slots each
+template <typename T>
+__global__ void k_code_number(const unsigned long long* __restrict__ keys, const T* __restrict__ vals,
+                              int* __restrict__ slot_code, T* __restrict__ tab, int* status) {
+    __shared__ int part[1024];
+    constexpr int per = kCodeSlots / 1024;
+    const int a = threadIdx.x * per;
+    int cnt = 0;
+    for (int q = a; q < a + per; ++q) cnt += keys[q] != 0;
+    part[threadIdx.x] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < 1024; ++t) {
+            const int c = part[t];
+            part[t] = run;
+            run += c;
+        }
+        status[1] = run;
+    }
+    __syncthreads();
+    int code = part[threadIdx.x];
+    for (int q = a; q < a + per; ++q) {
+        if (keys[q] == 0) {
+            slot_code[q] = -1;
+            continue;
+        }
+        slot_code[q] = code;
+        if (code < kMaxCodes) {
+            for (int grp = 0; grp < 3; ++grp) {
+                for (int c = 0; c < 3; ++c) tab[(long long)code * 12 + grp * 4 + c] = vals[(long long)q * 9 + grp * 3 + c];
+                tab[(long long)code * 12 + grp * 4 + 3] = T(0);
+            }
+        }
+        ++code;
+    }
+}
+
+template <typename T>
+__global__ void k_code_assign(const T* __restrict__ ch, const T* __restrict__ ce, const T* __restrict__ cl,
+                              long long N, const unsigned long long* __restrict__ keys,
+                              const int* __restrict__ slot_code, const T* __restrict__ tab,
+                              unsigned short* __restrict__ code, int* status) {
+    if (status[0]) return;  // too many triples: the context stays dense
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += stride) {
+        T v[9];
+        coef_triple<T>(ch, ce, cl, N, n, v);
+        const unsigned long long h = triple_hash<T>(v);
+        unsigned slot = (unsigned)h & (kCodeSlots - 1);
+        int c = -1;
+        for (int p = 0; p < kCodeProbes; ++p) {
+            const unsigned long long cur = keys[slot];
+            if (cur == h) {
+                c = slot_code[slot];
+                break;
+            }
+            if (cur == 0) break;
+            slot = (slot + 1) & (kCodeSlots - 1);
+        }
+        bool same = c >= 0 && c < kMaxCodes;
+        if (same) {
+            code[n] = (unsigned short)c;
+            for (int grp = 0; grp < 3; ++grp)
+                for (int q = 0; q < 3; ++q)
+                    same = same && word_bits(tab[(long long)c * 12 + grp * 4 + q]) == word_bits(v[grp * 3 + q]);
+        }
+        if (!same) atomicAdd(&status[2], 1);
+    }
+}
+
 template <typename T>
 __global__ void k_zero_ghosts(T* __restrict__ E, T* __restrict__ H, Geom g) {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -159,6 +159,9 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._coeff_dt = None
         self._sync_coeffs()
         self._kernels = "direct"
+        # coded coefficients for the fused step (see _ensure_codes)
+        self.coefficient_codes = os.environ.get("WAKIS_GB300_CODES", "1") != "0"
+        self.coefficient_code_count = 0
         self.kernels = os.environ.get("WAKIS_GB300_KERNELS", "auto")
 
         self.E._on_write = self._before_E_write
@@ -202,7 +205,19 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
     _fused_shapes = {}  # grid key -> ((vec, rows, zseg), times) chosen by tune_fused
 
     def _grid_key(self):
-        return (self.Nx, self.Ny, self.Nz, np.dtype(self.dtype).name, bool(self.use_conductivity))
+        return (self.Nx, self.Ny, self.Nz, np.dtype(self.dtype).name, bool(self.use_conductivity),
+                bool(self.coefficient_codes))
+
+    def _ensure_codes(self):
+        """Coded coefficients of the fused step (fit_set_coeff_codes): when
+        coefficient_codes is set, the distinct per-cell (ch, ce, cl) triples of the current
+        coefficients are found on the device once per coefficient set; a grid with at most
+        65535 of them then keeps a 16-bit code per cell and the fused step reads 2 bytes of
+        coefficients per cell instead of 9 words, with the same results.  Grids with more
+        distinct triples (strongly non-uniform spacing) stay dense."""
+        n = nat.C.c_int32(0)
+        self._ctx.call("fit_set_coeff_codes", int(bool(self.coefficient_codes)), nat.C.byref(n))
+        self.coefficient_code_count = int(n.value)
 
     def tune_fused(self, reps=5, zsegs=(2, 4, 8, 16, 32, 64, 128), force=False):
         """Autotuner of the fused step's tile shape for this grid: times every candidate
@@ -222,10 +237,14 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         if not vecs:
             raise ValueError("the fused step needs Nx to be a multiple of 2")
         self._sync_coeffs()
+        self._ensure_codes()
         times = {}
         ms = np.zeros(2)
+        budgets = ((4, 3), (4, 4), (8, 2))
+        if self.coefficient_code_count:
+            budgets += ((4, 5), (4, 6), (8, 3))  # the coded step needs fewer registers
         for vec in vecs:
-            for rows, ctas in ((4, 3), (4, 4), (8, 2)):
+            for rows, ctas in budgets:
                 for zseg in zsegs:
                     if zseg > self.Nz:
                         continue
