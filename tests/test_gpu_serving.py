@@ -167,7 +167,9 @@ def test_fused_pool_mix_with_odd_step_counts():
     every result agrees with its default wakesolve to rounding."""
     reqs = small_requests()
     refs = {r.tag: S.solve_alone(r, np.float32) for r in reqs}
-    jobs = [S.ServedSolve(r, kernels="auto") for r in reqs]
+    # even Nx: fused rows; the autotuner's choice between fused and two-pass on these
+    # small grids depends on timing, so the mix is set explicitly
+    jobs = [S.ServedSolve(r, kernels="fused" if r.n % 2 == 0 else "direct") for r in reqs]
     assert [j.solver.kernels for j in jobs] == ["fused", "fused", "direct", "fused"]
     pool = nat.Pool(8 << 30, chunk_steps=6)
     try:
