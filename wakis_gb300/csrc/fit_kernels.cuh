@@ -742,9 +742,9 @@ __global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __
 // Per cell the step moves the fused algorithmic bytes (E, H read and written once; ch,
 // ce and cl read once); halo reads of the neighbouring tiles hit L2.
 // planes ahead whose first-touch data (E of plane k+PF+1 along x and y, E_z, H and the
-// codes or coefficients of plane k+PF) a row warp asks L2 to fetch while it works on
-// plane k; 0: off.  On the 512x512x1024 pillbox (coded, 4 rows) distances 0, 1, 2, 3
-// ran 2.89, 2.62, 2.58 and 2.70 ms per step.
+// codes of plane k+PF) a row warp of the coded step asks L2 to fetch while it works on
+// plane k; 0: off.  On the 512x512x1024 pillbox (4 rows) distances 0, 1, 2, 3 ran 2.89,
+// 2.62, 2.58 and 2.70 ms per step; the same prefetch for the halo row gained nothing.
 #ifndef FIT_FUSED_PREFETCH
 #define FIT_FUSED_PREFETCH 2
 #endif
@@ -837,7 +837,7 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
             // the E update's coefficients do not depend on the new H: load them first so
             // their latency overlaps the H update and the barrier (coded: the codes; the
             // table entries are L1 hits, read after the barrier)
-            if constexpr (FIT_FUSED_PREFETCH > 0) {
+            if constexpr (CODED && FIT_FUSED_PREFETCH > 0) {
                 constexpr int PF = FIT_FUSED_PREFETCH;
                 if (k + PF + 1 < g.nz) {
                     prefetch_l2(Ein + n + (PF + 1) * g.sz);
@@ -849,16 +849,7 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
                     prefetch_l2(Hin + m);
                     prefetch_l2(Hin + g.N + m);
                     prefetch_l2(Hin + 2 * g.N + m);
-                    if constexpr (CODED) {
-                        prefetch_l2(code + m);
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            prefetch_l2(ch + c * g.N + m);
-                            prefetch_l2(ce + c * g.N + m);
-                            if constexpr (MODE == 1) prefetch_l2(cl + c * g.N + m);
-                        }
-                    }
+                    prefetch_l2(code + m);
                 }
             }
             if constexpr (CODED) {
