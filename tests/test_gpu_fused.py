@@ -87,11 +87,13 @@ def close(a, b, f64):
     return rel_l2(a, b) < (1e-12 if f64 else 1e-5)
 
 
+@pytest.mark.parametrize("kernels", ["fused", "direct"])
 @pytest.mark.parametrize("name", FUSED_CASES)
-def test_coded_coefficients_equal_dense(name, tmp_path, monkeypatch):
-    """The fused step with coded coefficients (a 16-bit code per cell into a table of the
-    exact (ch, ce, cl) triples) gives the dense fused step's results bit for bit."""
-    monkeypatch.setenv("WAKIS_GB300_KERNELS", "fused")
+def test_coded_coefficients_equal_dense(name, kernels, tmp_path, monkeypatch):
+    """The fused step and the two-pass kernels with coded coefficients (a 16-bit code per
+    cell into a table of the exact (ch, ce, cl) triples) give the dense kernels' results
+    bit for bit."""
+    monkeypatch.setenv("WAKIS_GB300_KERNELS", kernels)
     monkeypatch.setenv("WAKIS_GB300_CODES", "1")
     coded = run_case(name, tmpdir=tmp_path)
     monkeypatch.setenv("WAKIS_GB300_CODES", "0")

@@ -255,6 +255,11 @@ void launch_h(FitCtx* c) {
         allow_smem(k, sm);
         k<<<c->nsm, kTpbH, sm, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
                                        static_cast<const T*>(c->ch), c->g, metric<T>(c), c->d_err);
+    } else if (c->d_code) {
+        const long long nv = c->g.N / VEC;
+        k_hpass_coded<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E),
+                                                                   static_cast<T*>(c->H), c->g, metric<T>(c),
+                                                                   c->d_code, static_cast<const T*>(c->d_tab));
     } else {
         const long long nv = c->g.N / VEC;
         k_hpass<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
@@ -291,7 +296,14 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
     }
     const long long nv = c->g.N / VEC;
     const unsigned nb = grid1d(nv, 256);
-    if (mode == 0)
+    const T* tab = static_cast<const T*>(c->d_tab);
+    if (c->d_code && mode == 0)
+        k_epass_coded<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane,
+                                                         st, c->d_code, tab);
+    else if (c->d_code && mode == 1)
+        k_epass_coded<T, VEC, 1><<<nb, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane,
+                                                         st, c->d_code, tab);
+    else if (mode == 0)
         k_epass<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
     else if (mode == 1)
         k_epass<T, VEC, 1><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
@@ -367,9 +379,7 @@ bool fused_ok(const FitCtx* c, int mode) {
     return c->fused && c->E2 && c->H2 && mode != 2 && !c->plane.active && !c->abc_axes && pick_vec(c) >= 2;
 }
 
-// DENSE: also instantiate the dense-coefficient kernels (the coded kernels need fewer
-// registers, so the higher CTA counts per SM exist for them only)
-template <typename T, int VEC, int FY, int MB, bool DENSE = true>
+template <typename T, int VEC, int FY, int MB>
 void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
     constexpr int FX = 32 * VEC;
     const T* Ein = static_cast<const T*>(forward ? c->E : c->E2);
@@ -392,7 +402,7 @@ void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, c
     } else if (code) {
         k_step_fused<T, VEC, FY, MB, 0, true><<<grid, block, 0, c->own>>>(
             Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g, metric<T>(c), beam, st, zlen, code, tab);
-    } else if constexpr (DENSE) {
+    } else {
         if (mode == 1)
             k_step_fused<T, VEC, FY, MB, 1, false><<<grid, block, 0, c->own>>>(
                 Ein, Hin, Eout, Hout, ch, ce, cl, J, c->use_cond, c->g, metric<T>(c), beam, st, zlen, nullptr,
@@ -406,20 +416,14 @@ void launch_fused_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, c
 }
 
 // the fused step in the context's tile shape: fused_vec cells per thread, fused_rows rows,
-// register budget for fused_ctas CTAs per SM (8 rows: 2, coded also 3; 4 rows: 3 or 4,
-// coded also 5 or 6).  A coded-only budget on a dense context runs the nearest dense one.
+// register budget for fused_ctas CTAs per SM (8 rows: 2; 4 rows: 3 or 4).  Budgets of 5
+// or 6 CTAs per SM with 4 rows and 3 with 8 rows were timed for the coded step on the
+// 512x512x1024 pillbox (2.99 ms and more against 2.89 ms) and are not compiled.
 template <typename T, int VEC>
 void launch_fused_vec(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
-    const bool coded = c->d_code != nullptr;
-    if (c->fused_rows == 8 && c->fused_ctas == 3 && coded)
-        launch_fused_shape<T, VEC, 8, 3, false>(c, mode, st, forward, beam);
-    else if (c->fused_rows == 8)
+    if (c->fused_rows == 8)
         launch_fused_shape<T, VEC, 8, 2>(c, mode, st, forward, beam);
-    else if (c->fused_ctas == 6 && coded)
-        launch_fused_shape<T, VEC, 4, 6, false>(c, mode, st, forward, beam);
-    else if (c->fused_ctas == 5 && coded)
-        launch_fused_shape<T, VEC, 4, 5, false>(c, mode, st, forward, beam);
-    else if (c->fused_ctas >= 4)
+    else if (c->fused_ctas == 4)
         launch_fused_shape<T, VEC, 4, 4>(c, mode, st, forward, beam);
     else
         launch_fused_shape<T, VEC, 4, 3>(c, mode, st, forward, beam);
@@ -534,11 +538,24 @@ int build_codes_t(FitCtx* c, int32_t* ncodes) {
         return fail(c, FIT_ERR_CUDA, "coefficient codes: %s", cudaGetErrorString(e));
     }
     const bool ok = st[0] == 0 && st[1] <= kMaxCodes && st[2] == 0;
+    void* exact = nullptr;  // the table at its final size
+    if (ok) {
+        const size_t tb = (size_t)std::max(st[1], 1) * 12 * sizeof(T);
+        int rc2 = dev_alloc(c, &exact, tb);
+        if (!rc2) e = cudaMemcpyAsync(exact, tab, tb, cudaMemcpyDeviceToDevice, c->own);
+        if (rc2 || e != cudaSuccess) {
+            dfree(exact, c->own);
+            release(false);
+            return rc2 ? rc2 : fail(c, FIT_ERR_CUDA, "coefficient codes: %s", cudaGetErrorString(e));
+        }
+        dfree(tab, c->own);
+        tab = nullptr;
+    }
     release(ok);
     *ncodes = ok ? st[1] : 0;
     if (ok) {
         c->d_code = code;
-        c->d_tab = tab;
+        c->d_tab = exact;
         c->ncodes = st[1];
     }
     return FIT_OK;
@@ -1353,7 +1370,7 @@ int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg, int3
     if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     const bool vec_ok = (vec == 2 && c->g.nx % 2 == 0) || (vec == 4 && c->dtype == FIT_F32 && c->g.nx % 4 == 0);
     if (ctas == 0) ctas = rows == 8 ? 2 : 3;
-    const bool ctas_ok = (rows == 8 && (ctas == 2 || ctas == 3)) || (rows == 4 && ctas >= 3 && ctas <= 6);
+    const bool ctas_ok = (rows == 8 && ctas == 2) || (rows == 4 && (ctas == 3 || ctas == 4));
     if (!vec_ok || !ctas_ok || zseg < 1 || zseg > c->g.nz)
         return fail(c, FIT_ERR_ARG, "bad fused tile shape (vec %d, rows %d, z ranges %d, CTAs/SM %d)", vec, rows, zseg,
                     ctas);

@@ -560,13 +560,15 @@ __device__ __forceinline__ void hpass_eval(const T* __restrict__ E, const T* H, 
 }
 
 // H pass of the VEC cells starting at component-local flat index n
-template <typename T, int VEC>
+template <typename T, int VEC, bool CODED = false>
 __device__ __forceinline__ void hpass_at(const T* __restrict__ E, T* __restrict__ H, const T* __restrict__ ch,
-                                         const Geom& g, const Metric<T>& mt, long long n) {
+                                         const Geom& g, const Metric<T>& mt, long long n,
+                                         const unsigned short* __restrict__ code = nullptr,
+                                         const T* __restrict__ tab = nullptr) {
     int i0, j, k;
     cell_of(n, g, i0, j, k);
     T hx[VEC], hy[VEC], hz[VEC];
-    hpass_eval<T, VEC>(E, H, ch, g, mt, n, i0, j, k, hx, hy, hz);
+    hpass_eval<T, VEC, CODED>(E, H, ch, g, mt, n, i0, j, k, hx, hy, hz, code, tab);
     st_v<T, VEC>(H + n, hx);
     st_v<T, VEC>(H + g.N + n, hy);
     st_v<T, VEC>(H + 2 * g.N + n, hz);
@@ -580,6 +582,16 @@ __global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __
     hpass_at<T, VEC>(E, H, ch, g, mt, v * VEC);
 }
 
+// the H pass with coded coefficients (ch from the code table)
+template <typename T, int VEC>
+__global__ void __launch_bounds__(256, 3) k_hpass_coded(const T* __restrict__ E, T* __restrict__ H, Geom g,
+                                                     Metric<T> mt, const unsigned short* __restrict__ code,
+                                                     const T* __restrict__ tab) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.N / VEC) return;
+    hpass_at<T, VEC, true>(E, H, nullptr, g, mt, v * VEC, code, tab);
+}
+
 // MODE 0: E += ce*(C^T ĥ)                       (no conduction current)
 // MODE 1: E = cl*E + ce*(C^T ĥ)                 (J = sigma*E_prev folded into cl)
 // MODE 2: E = E + ce*(C^T ĥ) - cj*J; J = sg*E   (explicit J; J written if conductive)
@@ -588,7 +600,8 @@ __global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __
 // them: own (hx, hy, hz), the row below (hxy, hzy at n - Nx), the plane below (hxz, hyz
 // at n - Nx*Ny) and the value before the vector along x (hyx, hzx at n - 1).  E is read
 // from Esrc and written to Edst (the same array for the in-place passes).
-template <typename T, int VEC, int MODE>
+// CODED (MODE 0 and 1): ce and cl come from the code table (code, tab)
+template <typename T, int VEC, int MODE, bool CODED = false>
 __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&hx)[VEC], const T (&hy)[VEC],
                                              const T (&hz)[VEC], const T (&hxy)[VEC], const T (&hzy)[VEC],
                                              const T (&hxz)[VEC], const T (&hyz)[VEC], T hyx, T hzx,
@@ -596,16 +609,24 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
                                              const T* __restrict__ cj, const T* __restrict__ sg, int use_cond,
                                              const Geom& g, const Metric<T>& mt, const BeamArgs& b,
                                              const PlaneArgs& pl, const StepArgs& st, long long n, int i0, int j,
-                                             int k) {
+                                             int k, const unsigned short* __restrict__ code = nullptr,
+                                             const T* __restrict__ tab = nullptr) {
+    static_assert(!(CODED && MODE == 2), "the explicit-J pass reads dense coefficients");
     T cur[3][VEC];
     epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
     T ex[VEC], ey[VEC], ez[VEC], kx[VEC], ky[VEC], kz[VEC];
+    [[maybe_unused]] unsigned cd[VEC];
     ld_v<T, VEC>(ex, Esrc + n);
     ld_v<T, VEC>(ey, Esrc + g.N + n);
     ld_v<T, VEC>(ez, Esrc + 2 * g.N + n);
-    ldg_v<T, VEC>(kx, ce + n);
-    ldg_v<T, VEC>(ky, ce + g.N + n);
-    ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+    if constexpr (CODED) {
+        ld_codes<VEC>(cd, code + n);
+        tab_get_v<T, VEC>(tab, cd, 1, kx, ky, kz);
+    } else {
+        ldg_v<T, VEC>(kx, ce + n);
+        ldg_v<T, VEC>(ky, ce + g.N + n);
+        ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+    }
     if constexpr (MODE == 2) {
         const bool on_line = b.active && (j == b.iys) && (b.ixs >= i0) && (b.ixs < i0 + VEC);
         double jb = 0.0;
@@ -652,7 +673,9 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
         }
     } else {
         T lx[VEC], ly[VEC], lz[VEC];
-        if constexpr (MODE == 1) {
+        if constexpr (MODE == 1 && CODED) {
+            tab_get_v<T, VEC>(tab, cd, 2, lx, ly, lz);
+        } else if constexpr (MODE == 1) {
             ldg_v<T, VEC>(lx, cl + n);
             ldg_v<T, VEC>(ly, cl + g.N + n);
             ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
@@ -669,11 +692,13 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
 }
 
 
-template <typename T, int VEC, int MODE>
+template <typename T, int VEC, int MODE, bool CODED = false>
 __device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict__ H, const T* __restrict__ ce,
                                          const T* __restrict__ cl, T* __restrict__ J, const T* __restrict__ cj,
                                          const T* __restrict__ sg, int use_cond, const Geom& g, const Metric<T>& mt,
-                                         const BeamArgs& b, const PlaneArgs& pl, const StepArgs& st, long long n) {
+                                         const BeamArgs& b, const PlaneArgs& pl, const StepArgs& st, long long n,
+                                         const unsigned short* __restrict__ code = nullptr,
+                                         const T* __restrict__ tab = nullptr) {
     int i0, j, k;
     cell_of(n, g, i0, j, k);
     const T* Hx = H;
@@ -705,8 +730,8 @@ __device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict_
         hyx = __ldg(Hy + n - 1);
         hzx = __ldg(Hz + n - 1);
     }
-    epass_finish<T, VEC, MODE>(E, E, hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, ce, cl, J, cj, sg, use_cond, g, mt, b,
-                               pl, st, n, i0, j, k);
+    epass_finish<T, VEC, MODE, CODED>(E, E, hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, ce, cl, J, cj, sg, use_cond, g,
+                                      mt, b, pl, st, n, i0, j, k, code, tab);
 }
 
 template <typename T, int VEC, int MODE>
@@ -718,6 +743,19 @@ __global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.N / VEC) return;
     epass_at<T, VEC, MODE>(E, H, ce, cl, J, cj, sg, use_cond, g, mt, b, pl, st, v * VEC);
+}
+
+// the E pass (MODE 0 or 1) with coded coefficients (ce, cl from the code table)
+template <typename T, int VEC, int MODE>
+__global__ void __launch_bounds__(256, 3) k_epass_coded(T* __restrict__ E, const T* __restrict__ H,
+                                                     T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
+                                                     BeamArgs b, PlaneArgs pl, StepArgs st,
+                                                     const unsigned short* __restrict__ code,
+                                                     const T* __restrict__ tab) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.N / VEC) return;
+    epass_at<T, VEC, MODE, true>(E, H, nullptr, nullptr, J, nullptr, nullptr, use_cond, g, mt, b, pl, st, v * VEC,
+                                 code, tab);
 }
 
 // ---------------------------------------------------------------- fused step (2.5-D)
@@ -1812,6 +1850,8 @@ struct PoolInst {
     int fused;        // 1: stepped by k_step_fused_pool
     int tiles_x, tiles_y;  // fused tile grid of one z range
     int pad0, pad1;
+    const unsigned short* code;  // coded coefficients of the two-pass classes (nullptr: dense)
+    const T* tab;
 };
 
 template <typename T>
@@ -1877,7 +1917,10 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_hpass_pool(const PoolTable<T
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
     pool_walk<T, VEC>(tab, si, sn, [](const PoolInst<T>& d, long long v) {
-        hpass_at<T, VEC>(d.E, d.H, d.ch, d.g, d.mt, v * VEC);
+        if (d.code)
+            hpass_at<T, VEC, true>(d.E, d.H, d.ch, d.g, d.mt, v * VEC, d.code, d.tab);
+        else
+            hpass_at<T, VEC>(d.E, d.H, d.ch, d.g, d.mt, v * VEC);
     });
 }
 
@@ -1891,9 +1934,15 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T
         st.vt_table = d.vt_table;
         st.vt_len = d.vt_len;
         const PlaneArgs pl{};
-        if (d.mode == 1)
+        if (d.mode == 1 && d.code)
+            epass_at<T, VEC, 1, true>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl,
+                                      st, v * VEC, d.code, d.tab);
+        else if (d.mode == 1)
             epass_at<T, VEC, 1>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl, st,
                                 v * VEC);
+        else if (d.code)
+            epass_at<T, VEC, 0, true>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl,
+                                      st, v * VEC, d.code, d.tab);
         else
             epass_at<T, VEC, 0>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl, st,
                                 v * VEC);

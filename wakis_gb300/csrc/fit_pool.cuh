@@ -536,6 +536,10 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     r.ce = static_cast<const float*>(c->ce);
     r.cl = static_cast<const float*>(c->cl);
     r.J = static_cast<float*>(c->J);
+    // the two-pass classes read the context's coefficient codes when it has them (the
+    // pooled fused class keeps the dense arrays)
+    r.code = fused ? nullptr : c->d_code;
+    r.tab = fused ? nullptr : static_cast<const float*>(c->d_tab);
     r.beam = c->beam;
     r.tap = c->tap;
     r.d_step = c->d_step;

@@ -307,8 +307,7 @@ class RoutinesMixin:
             self._set_ghosts_to_0()
             self.step_0 = False
         self._sync_coeffs()
-        if self._kernels == "fused":
-            self._ensure_codes()
+        self._ensure_codes()
         if self._kernels == "fused" and nsteps >= 256:
             self.tune_fused()  # once per grid shape; leaves the fields unchanged
         self._ctx.call("fit_run", n0, nsteps)

@@ -87,14 +87,14 @@ def config3_requests(count=64, seed=3, rate_hz=None, wakelength=1.0):
 def footprint_bytes(req, dtype=np.float32, kernels="direct"):
     """Device bytes a request holds while it is served: E, H, J (3 x 3N field words), the
     FP64 material tensors ieps, imu, sigma (3 x 3N x 8), the library's coefficient arrays
-    (ch, ce and, with losses, cl: 3N field words each), with the fused step the second
-    E and H buffers (6N field words), the cell mask and a fixed allowance for the 1-D
-    metrics, tap tables and allocator rounding."""
+    (ch, ce and, with losses, cl: 3N field words each) and their 2-byte codes, with the
+    fused step the second E and H buffers (6N field words), the cell mask and a fixed
+    allowance for the 1-D metrics, tap tables, the code table and allocator rounding."""
     N = req.cells
     w = np.dtype(dtype).itemsize
     ncoef = 3 if req.lossy else 2
     fused = kernels == "fused" or (kernels == "auto" and req.n % 2 == 0)
-    return int(N * (9 * w + 72 + 3 * w * ncoef + 1 + (6 * w if fused else 0)) + 8 * 2 ** 20)
+    return int(N * (9 * w + 72 + 3 * w * ncoef + 1 + 2 + (6 * w if fused else 0)) + 8 * 2 ** 20)
 
 
 def _axes(req):
@@ -166,6 +166,7 @@ class ServedSolve:
             s._set_ghosts_to_0()
             s.step_0 = False
         s._sync_coeffs()
+        s._ensure_codes()  # the pool's two-pass classes read the coefficient codes
 
     def submit(self, pool):
         pool.submit(self.solver._ctx, self.first, self.Nt - self.first, self.req.tag)

@@ -240,11 +240,8 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._ensure_codes()
         times = {}
         ms = np.zeros(2)
-        budgets = ((4, 3), (4, 4), (8, 2))
-        if self.coefficient_code_count:
-            budgets += ((4, 5), (4, 6), (8, 3))  # the coded step needs fewer registers
         for vec in vecs:
-            for rows, ctas in budgets:
+            for rows, ctas in ((4, 3), (4, 4), (8, 2)):
                 for zseg in zsegs:
                     if zseg > self.Nz:
                         continue
