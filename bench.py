@@ -586,14 +586,19 @@ def run_serve(args):
         pool.close()
         cu = sum(j.req.cells * (j.Nt - j.first) for j in jobs)
         mbs = sum(work_bytes[j.req.tag] * j.req.cells * (j.Nt - j.first) for j in jobs)
-        two_pass = sum((108 if j.req.lossy else 96) * j.req.cells * (j.Nt - j.first) for j in jobs)
+        # bytes the pool's two-pass kernels move per cell-update: coded 76 B (E and H read
+        # and written once per pass, a 2-byte code per pass), dense 96 B (PEC) / 108 B (lossy)
+        coded = [j.solver.coefficient_code_count > 0 for j in jobs]
+        two_pass = sum((76 if cd else (108 if j.req.lossy else 96)) * j.req.cells * (j.Nt - j.first)
+                       for j, cd in zip(jobs, coded))
         out["pool_all_resident"] = {"requests": len(jobs), "seconds": el, "mcell_updates_per_s": cu / el / 1e6,
                                     "hbm_gbs_model": mbs / el / 1e9, "hbm_frac_model": mbs / el / 1e9 / peak,
                                     "hbm_gbs_two_pass": two_pass / el / 1e9,
                                     "hbm_frac_two_pass": two_pass / el / 1e9 / peak,
+                                    "coded_requests": int(sum(coded)),
                                     "chunks": st["chunks"], "variant": st["variant"], "grid": st["grid"],
-                                    "note": "72 B (PEC) / 84 B (lossy) per cell-update model; the two-pass "
-                                            "kernels move 96 / 108 B"}
+                                    "note": "72 B (PEC) / 84 B (lossy) per cell-update model; the coded two-pass "
+                                            "kernels move 76 B (dense 96 / 108 B)"}
         for j in jobs:
             j.close()
         del jobs

@@ -225,12 +225,14 @@ FIT_API int fit_set_kernel_variant(FitCtx *ctx, int32_t variant);
 /* Coded coefficients for the fused step; no counterpart in the reference.  enable != 0:
  * the context finds the distinct per-cell triples (ch, ce, cl) of its coefficient arrays
  * on the device and, when there are at most 65535 of them, stores one 16-bit code per
- * cell and a table of the exact triples; the fused step then reads 2 bytes of
- * coefficients per cell instead of 9 words, with bit-identical results.  Every cell's
+ * cell and a table of the exact triples; the fused step and the two-pass passes (not the
+ * FIT_J_EXPLICIT E pass) then read 2 bytes of coefficients per cell instead of 3 to 9
+ * words, with bit-identical results.  Contexts submitted to a pool keep their codes for
+ * the pool's two-pass classes.  Every cell's
  * code is checked against its triple before the codes are used.  *ncodes (may be NULL)
  * receives the number of distinct triples, or 0 when the context stays dense (too many
  * triples).  fit_set_coeffs drops the codes; enable == 0 drops them too.  Needs
- * N*2 bytes plus a table of at most 65535*12 words of device memory. */
+ * N*2 bytes plus a table of 12 words per code (during the build about 14 MB more). */
 FIT_API int fit_set_coeff_codes(FitCtx *ctx, int32_t enable, int32_t *ncodes);
 
 /* Tile shape of the fused step: vec cells per thread along x (2, or 4 for FP32; Nx must
