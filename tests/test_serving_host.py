@@ -39,7 +39,7 @@ def test_footprint_counts_fields_materials_and_coefficients():
     r = S.CavityRequest(tag=0, side=0.04, rp=0.005, n=100, sigmaz=0.01, sigma=0.0)
     N = r.cells
     f32 = S.footprint_bytes(r, np.float32)
-    assert f32 == N * (36 + 72 + 24 + 1) + 8 * 2 ** 20
+    assert f32 == N * (36 + 72 + 24 + 1 + 2) + 8 * 2 ** 20  # ... + mask byte + 2-byte coefficient code
     lossy = S.CavityRequest(tag=1, side=0.04, rp=0.005, n=100, sigmaz=0.01, sigma=1e4)
     assert S.footprint_bytes(lossy, np.float32) - f32 == 12 * N
     assert S.footprint_bytes(r, np.float64) > f32
