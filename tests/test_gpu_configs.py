@@ -81,3 +81,15 @@ def test_config1_fp32_against_fp64(name, tmp_path):
     np.testing.assert_array_equal(r32["s"], r64["s"])
     assert rel_l2(r32["WP"], r64["WP"]) < 1e-4
     assert rel_l2(r32["Z"], r64["Z"]) < 1e-4
+
+
+def test_config1_coded_equals_dense(tmp_path, monkeypatch):
+    """The full config-1 run (128x128x256, lossy walls, PML, 4452 steps) with coded
+    coefficients gives the dense run's wake bit for bit."""
+    case = C.CONFIGS["config1a"]
+    out = {}
+    for codes in ("1", "0"):
+        monkeypatch.setenv("WAKIS_GB300_CODES", codes)
+        out[codes] = run_case("config1a", case=case, tmpdir=tmp_path, dtype=np.float32)
+    for k in ("WP", "Z", "WPx", "WPy", "E", "H"):
+        np.testing.assert_array_equal(out["1"][k], out["0"][k], err_msg=k)
