@@ -137,19 +137,44 @@ __device__ __forceinline__ T edge_len(const T* const* L, int d, int i, int j, in
     return d == 0 ? L[0][i] : (d == 1 ? L[1][j] : L[2][k]);
 }
 
+// Explicitly rounded arithmetic of the stencils: one rounding per multiply, add and
+// fused multiply-add, in a fixed pattern.  Every kernel that inlines the stencil
+// functions (fused or two-pass, coded or dense coefficients) then computes the same bits,
+// whatever multiply-adds the compiler would have contracted in each of them.
+template <typename T>
+__device__ __forceinline__ T rmul(T a, T b) {
+    if constexpr (sizeof(T) == 4) return __fmul_rn(a, b);
+    else return __dmul_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T radd(T a, T b) {
+    if constexpr (sizeof(T) == 4) return __fadd_rn(a, b);
+    else return __dadd_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T rsub(T a, T b) {
+    if constexpr (sizeof(T) == 4) return __fsub_rn(a, b);
+    else return __dsub_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T rfma(T a, T b, T c) {  // a*b + c
+    if constexpr (sizeof(T) == 4) return __fmaf_rn(a, b, c);
+    else return __fma_rn(a, b, c);
+}
+
 // ê_d(m) = Dbc_pec * L_d * E_d[m]  (column scaling of C by Ds and Dbc)
 template <typename T>
 __device__ __forceinline__ T ehat(T e, int d, const Nb& p, const Geom& g, const Metric<T>& m) {
     if (!p.valid) return T(0);
     if (!face_open(g.pec, d, p.i, p.j, p.k, g)) return T(0);
-    return edge_len<T>(m.L, d, p.i, p.j, p.k) * e;
+    return rmul(edge_len<T>(m.L, d, p.i, p.j, p.k), e);
 }
 // ĥ_d(m) = Dbc_pmc * tL_d * H_d[m]
 template <typename T>
 __device__ __forceinline__ T hhat(T h, int d, const Nb& p, const Geom& g, const Metric<T>& m) {
     if (!p.valid) return T(0);
     if (!face_open(g.pmc, d, p.i, p.j, p.k, g)) return T(0);
-    return edge_len<T>(m.tL, d, p.i, p.j, p.k) * h;
+    return rmul(edge_len<T>(m.tL, d, p.i, p.j, p.k), h);
 }
 
 // ---------------------------------------------------------------- vector loads/stores
@@ -344,12 +369,12 @@ __device__ __forceinline__ void hpass_cells(const T (&ex)[VEC], const T (&ey)[VE
             const T lyn = (e + 1 < VEC) ? ly : lyl;
             const T eyX = (e + 1 < VEC) ? ey[e + 1] : eyx;
             const T ezX = (e + 1 < VEC) ? ez[e + 1] : ezx;
-            const T curlx = me * (ly * (ey[e] - eyz[e]) + lz * (ezy[e] - ez[e]));
-            const T curly = lx * (exz[e] - ex[e]) + lz * (me * ez[e] - mn * ezX);
-            const T curlz = lx * (ex[e] - exy[e]) + (mn * lyn * eyX - me * ly * ey[e]);
-            hx[e] = hx[e] - cx[e] * curlx;
-            hy[e] = hy[e] - cy[e] * curly;
-            hz[e] = hz[e] - cz[e] * curlz;
+            const T curlx = rmul(me, rfma(ly, rsub(ey[e], eyz[e]), rmul(lz, rsub(ezy[e], ez[e]))));
+            const T curly = rfma(lx, rsub(exz[e], ex[e]), rmul(lz, rfma(me, ez[e], -rmul(mn, ezX))));
+            const T curlz = rfma(lx, rsub(ex[e], exy[e]), rfma(rmul(mn, lyn), eyX, -rmul(rmul(me, ly), ey[e])));
+            hx[e] = rfma(-cx[e], curlx, hx[e]);
+            hy[e] = rfma(-cy[e], curly, hy[e]);
+            hz[e] = rfma(-cz[e], curlz, hz[e]);
         }
         return;
     }
@@ -373,12 +398,12 @@ __device__ __forceinline__ void hpass_cells(const T (&ex)[VEC], const T (&ey)[VE
         const T eyX = ehat<T>((e + 1 < VEC) ? ey[e + 1] : eyx, 1, pxi, g, mt);
         const T ezX = ehat<T>((e + 1 < VEC) ? ez[e + 1] : ezx, 2, pxi, g, mt);
         // (C ê)_x = -D_z ê_y + D_y ê_z ; (C ê)_y = D_z ê_x - D_x ê_z ; (C ê)_z = -D_y ê_x + D_x ê_y
-        const T curlx = (ey0 - eyZ) + (ezY - ez0);
-        const T curly = (exZ - ex0) + (ez0 - ezX);
-        const T curlz = (ex0 - exY) + (eyX - ey0);
-        hx[e] = hx[e] - cx[e] * curlx;
-        hy[e] = hy[e] - cy[e] * curly;
-        hz[e] = hz[e] - cz[e] * curlz;
+        const T curlx = radd(rsub(ey0, eyZ), rsub(ezY, ez0));
+        const T curly = radd(rsub(exZ, ex0), rsub(ez0, ezX));
+        const T curlz = radd(rsub(ex0, exY), rsub(eyX, ey0));
+        hx[e] = rfma(-cx[e], curlx, hx[e]);
+        hy[e] = rfma(-cy[e], curly, hy[e]);
+        hz[e] = rfma(-cz[e], curlz, hz[e]);
     }
 }
 
@@ -405,9 +430,9 @@ __device__ __forceinline__ void epass_curl(const T (&hx)[VEC], const T (&hy)[VEC
             const T lyp = (e > 0) ? ly : lyf;
             const T hyX = (e > 0) ? hy[e - 1] : hyx;
             const T hzX = (e > 0) ? hz[e - 1] : hzx;
-            cur[0][e] = mpe * (ly * (hyz[e] - hy[e]) + lz * (hz[e] - hzy[e]));
-            cur[1][e] = lx * (hx[e] - hxz[e]) + lz * (mpp * hzX - mpe * hz[e]);
-            cur[2][e] = lx * (hxy[e] - hx[e]) + (mpe * ly * hy[e] - mpp * lyp * hyX);
+            cur[0][e] = rmul(mpe, rfma(ly, rsub(hyz[e], hy[e]), rmul(lz, rsub(hz[e], hzy[e]))));
+            cur[1][e] = rfma(lx, rsub(hx[e], hxz[e]), rmul(lz, rfma(mpp, hzX, -rmul(mpe, hz[e]))));
+            cur[2][e] = rfma(lx, rsub(hxy[e], hx[e]), rfma(rmul(mpe, ly), hy[e], -rmul(rmul(mpp, lyp), hyX)));
         }
         return;
     }
@@ -432,9 +457,9 @@ __device__ __forceinline__ void epass_curl(const T (&hx)[VEC], const T (&hy)[VEC
         const T hzX = hhat<T>((e > 0) ? hz[e - 1] : hzx, 2, pxi, g, mt);
         // (C^T ĥ)_x = D^T_z ĥ_y - D^T_y ĥ_z ; (C^T ĥ)_y = -D^T_z ĥ_x + D^T_x ĥ_z ;
         // (C^T ĥ)_z = D^T_y ĥ_x - D^T_x ĥ_y
-        cur[0][e] = (hyZ - hy0) + (hz0 - hzY);
-        cur[1][e] = (hx0 - hxZ) + (hzX - hz0);
-        cur[2][e] = (hxY - hx0) + (hy0 - hyX);
+        cur[0][e] = radd(rsub(hyZ, hy0), rsub(hz0, hzY));
+        cur[1][e] = radd(rsub(hx0, hxZ), rsub(hzX, hz0));
+        cur[2][e] = radd(rsub(hxY, hx0), rsub(hy0, hyX));
     }
 }
 
@@ -458,9 +483,9 @@ __device__ __forceinline__ void epass_update(T (&ex)[VEC], T (&ey)[VEC], T (&ez)
     if constexpr (MODE == 0) {
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
-            ex[e] = ex[e] + kx[e] * cur[0][e];
-            ey[e] = ey[e] + ky[e] * cur[1][e];
-            ez[e] = ez[e] + kz[e] * cur[2][e];
+            ex[e] = rfma(kx[e], cur[0][e], ex[e]);
+            ey[e] = rfma(ky[e], cur[1][e], ey[e]);
+            ez[e] = rfma(kz[e], cur[2][e], ez[e]);
         }
     } else {
         // on the hard-source plane the conduction current is sigma times the E_x the
@@ -470,20 +495,21 @@ __device__ __forceinline__ void epass_update(T (&ex)[VEC], T (&ey)[VEC], T (&ez)
         for (int e = 0; e < VEC; ++e) {
             const int i = i0 + e;
             if (on_plane && i >= pl.x0 && i < pl.x1)
-                ex[e] = (ex[e] - (T(1) - lx[e]) * (T)pl.stash[(i - pl.x0) + (j - pl.y0) * (pl.x1 - pl.x0)]) +
-                        kx[e] * cur[0][e];
+                ex[e] = rfma(kx[e], cur[0][e],
+                             rsub(ex[e], rmul(rsub(T(1), lx[e]),
+                                              (T)pl.stash[(i - pl.x0) + (j - pl.y0) * (pl.x1 - pl.x0)])));
             else
-                ex[e] = lx[e] * ex[e] + kx[e] * cur[0][e];
-            ey[e] = ly[e] * ey[e] + ky[e] * cur[1][e];
+                ex[e] = rfma(kx[e], cur[0][e], rmul(lx[e], ex[e]));
+            ey[e] = rfma(ky[e], cur[1][e], rmul(ly[e], ey[e]));
             // on the beam line J was overwritten by the beam: no sigma*E term there
-            ez[e] = ((on_line && (i0 + e == b.ixs)) ? ez[e] : lz[e] * ez[e]) + kz[e] * cur[2][e];
+            ez[e] = rfma(kz[e], cur[2][e], (on_line && (i0 + e == b.ixs)) ? ez[e] : rmul(lz[e], ez[e]));
         }
     }
     if (on_line) {
-        const T dj = (T)b.dtieps[k] * (T)jb;
+        const T dj = rmul((T)b.dtieps[k], (T)jb);
 #pragma unroll
         for (int e = 0; e < VEC; ++e)
-            if (i0 + e == b.ixs) ez[e] = ez[e] - dj;
+            if (i0 + e == b.ixs) ez[e] = rsub(ez[e], dj);
         if (!use_cond) J[2 * g.N + n + (b.ixs - i0)] = (T)jb;  // J keeps the last beam value
     }
 }
@@ -650,9 +676,9 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
         }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
-            ex[e] = ex[e] + kx[e] * cur[0][e] - ax[e] * jx[e];
-            ey[e] = ey[e] + ky[e] * cur[1][e] - ay[e] * jy[e];
-            ez[e] = ez[e] + kz[e] * cur[2][e] - az[e] * jz[e];
+            ex[e] = rfma(-ax[e], jx[e], rfma(kx[e], cur[0][e], ex[e]));
+            ey[e] = rfma(-ay[e], jy[e], rfma(ky[e], cur[1][e], ey[e]));
+            ez[e] = rfma(-az[e], jz[e], rfma(kz[e], cur[2][e], ez[e]));
         }
         if (use_cond) {
             T sx[VEC], sy_[VEC], szz[VEC];
@@ -661,9 +687,9 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
             ldg_v<T, VEC>(szz, sg + 2 * g.N + n);
 #pragma unroll
             for (int e = 0; e < VEC; ++e) {
-                jx[e] = sx[e] * ex[e];
-                jy[e] = sy_[e] * ey[e];
-                jz[e] = szz[e] * ez[e];
+                jx[e] = rmul(sx[e], ex[e]);
+                jy[e] = rmul(sy_[e], ey[e]);
+                jz[e] = rmul(szz[e], ez[e]);
             }
             st_v<T, VEC>(J + n, jx);
             st_v<T, VEC>(J + g.N + n, jy);
