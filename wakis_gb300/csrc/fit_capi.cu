@@ -247,6 +247,29 @@ void allow_smem(KernelPtr k, size_t bytes) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// vectors between a thread and its counterpart in the next resident wave of CTAs of a
+// coded two-pass kernel (its L2 prefetch distance); 0 turns the prefetch off.  The
+// 1-wide kernels go without: their prefetch did not pay in the serving pool.
+#ifndef FIT_TWO_PASS_PREFETCH
+#define FIT_TWO_PASS_PREFETCH 1
+#endif
+template <typename T, int VEC>
+long long coded_ahead(const FitCtx* c, bool e_pass) {
+    if (VEC < 2 || !FIT_TWO_PASS_PREFETCH) return 0;
+    // resident CTAs per SM of each kernel, queried once (no stream work: safe during capture)
+    static const int occ_h = [] {
+        int o = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_hpass_coded<T, VEC>, 256, 0) == cudaSuccess ? o : 0;
+    }();
+    static const int occ_e = [] {
+        int o = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_epass_coded<T, VEC, 1>, 256, 0) == cudaSuccess ? o
+                                                                                                              : 0;
+    }();
+    const int occ = e_pass ? occ_e : occ_h;
+    return occ > 0 ? (long long)c->nsm * occ * 256 : 0;
+}
+
 template <typename T, int VEC>
 void launch_h(FitCtx* c) {
     if (VEC * sizeof(T) == 16 && staged_ok(c)) {
@@ -259,7 +282,8 @@ void launch_h(FitCtx* c) {
         const long long nv = c->g.N / VEC;
         k_hpass_coded<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E),
                                                                    static_cast<T*>(c->H), c->g, metric<T>(c),
-                                                                   c->d_code, static_cast<const T*>(c->d_tab));
+                                                                   c->d_code, static_cast<const T*>(c->d_tab),
+                                                                   coded_ahead<T, VEC>(c, false));
     } else {
         const long long nv = c->g.N / VEC;
         k_hpass<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
@@ -299,10 +323,10 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
     const T* tab = static_cast<const T*>(c->d_tab);
     if (c->d_code && mode == 0)
         k_epass_coded<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane,
-                                                         st, c->d_code, tab);
+                                                         st, c->d_code, tab, coded_ahead<T, VEC>(c, true));
     else if (c->d_code && mode == 1)
         k_epass_coded<T, VEC, 1><<<nb, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane,
-                                                         st, c->d_code, tab);
+                                                         st, c->d_code, tab, coded_ahead<T, VEC>(c, true));
     else if (mode == 0)
         k_epass<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, ce, cl, J, cj, sg, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st);
     else if (mode == 1)

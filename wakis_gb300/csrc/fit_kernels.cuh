@@ -178,6 +178,8 @@ __device__ __forceinline__ T hhat(T h, int d, const Nb& p, const Geom& g, const 
 }
 
 // ---------------------------------------------------------------- vector loads/stores
+// a hint that the line holding p will be read soon: fetched into L2, nothing waits on it
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 template <typename T, int VEC>
 __device__ __forceinline__ void ldg_v(T (&r)[VEC], const T* __restrict__ p) {
     if constexpr (VEC == 4 && sizeof(T) == 4) {
@@ -608,13 +610,24 @@ __global__ void __launch_bounds__(256, 3) k_hpass(const T* __restrict__ E, T* __
     hpass_at<T, VEC>(E, H, ch, g, mt, v * VEC);
 }
 
-// the H pass with coded coefficients (ch from the code table)
+// the H pass with coded coefficients (ch from the code table).  ahead > 0: the thread
+// first asks L2 for E, H and the code of the vector `ahead` vectors on, the one a thread
+// of the next resident wave of CTAs works on.
 template <typename T, int VEC>
 __global__ void __launch_bounds__(256, 3) k_hpass_coded(const T* __restrict__ E, T* __restrict__ H, Geom g,
                                                      Metric<T> mt, const unsigned short* __restrict__ code,
-                                                     const T* __restrict__ tab) {
+                                                     const T* __restrict__ tab, long long ahead) {
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.N / VEC) return;
+    if (ahead > 0 && (v + ahead) * VEC < g.N) {
+        const long long m = (v + ahead) * VEC;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            prefetch_l2(E + c * g.N + m);
+            prefetch_l2(H + c * g.N + m);
+        }
+        prefetch_l2(code + m);
+    }
     hpass_at<T, VEC, true>(E, H, nullptr, g, mt, v * VEC, code, tab);
 }
 
@@ -777,9 +790,18 @@ __global__ void __launch_bounds__(256, 3) k_epass_coded(T* __restrict__ E, const
                                                      T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
                                                      BeamArgs b, PlaneArgs pl, StepArgs st,
                                                      const unsigned short* __restrict__ code,
-                                                     const T* __restrict__ tab) {
+                                                     const T* __restrict__ tab, long long ahead) {
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.N / VEC) return;
+    if (ahead > 0 && (v + ahead) * VEC < g.N) {  // as in k_hpass_coded
+        const long long m = (v + ahead) * VEC;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            prefetch_l2(E + c * g.N + m);
+            prefetch_l2(H + c * g.N + m);
+        }
+        prefetch_l2(code + m);
+    }
     epass_at<T, VEC, MODE, true>(E, H, nullptr, nullptr, J, nullptr, nullptr, use_cond, g, mt, b, pl, st, v * VEC,
                                  code, tab);
 }
@@ -813,7 +835,6 @@ __global__ void __launch_bounds__(256, 3) k_epass_coded(T* __restrict__ E, const
 #define FIT_FUSED_PREFETCH 2
 #endif
 
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 template <typename T, int VEC, int FY>
 struct FusedShared {
