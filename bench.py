@@ -276,7 +276,9 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    clk_path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
+    # the nvidia-smi samples of the timed region (summarised into the line's "clocks")
+    clk_dir = os.environ.get("WAKIS_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+    clk_path = os.path.join(clk_dir, f"clocks_rank{rank}.csv")
     os.makedirs(os.path.dirname(clk_path), exist_ok=True)
     launches0 = nat.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

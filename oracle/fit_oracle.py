@@ -3,7 +3,7 @@
 This module is a numpy/scipy restatement of the reference's algorithm for the hot
 path (grid metrics, boundary handling, materials, PML, time step, the sparse-matrix
 leapfrog step, the beam / plane-wave sources, the wakesolve / emsolve drivers and the
-wake-potential / impedance post-processing).  It is the checker the parity tests
+wake-potential / impedance post-processing).  It is the reference the parity tests
 compare the CUDA path against, and the CPU baseline that ``bench.py`` times.  Only
 ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference
 legs may import it; the product package ``wakis_gb300`` never does.

@@ -272,7 +272,7 @@ def resonator_H(N, dt):
 
 
 # ----------------------------------------------------------------------------- full configs
-# The BASELINE workloads at full size (geometry analytic, evaluated at cell centres).
+# The benchmark workloads at full size (geometry analytic, evaluated at cell centres).
 CONFIGS = {
     # config 0: plain FP64 PEC cubic cavity, 60x60x120, ABC in z, CFL 1.0, wake 0.5 m, fmax 5 GHz
     "config0": dict(

@@ -1,4 +1,4 @@
-"""Parity and accuracy at the BASELINE workloads themselves (full size):
+"""Parity and accuracy at the benchmark workloads themselves (full size):
 
 * config 0 (FP64, 60x60x120, 1220 steps): the CUDA path against the CPU oracle within
   1e-10 relative L2 on WP, Z and the final fields;
