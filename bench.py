@@ -5,18 +5,20 @@ Workload (default): the large single-domain roofline run -- lossy pillbox cavity
 10 mm beam pipe to z = +-200 mm on a 512 x 512 x 1024 grid (268 M cells), FP32 fields,
 16-cell PML at both z ends, Gaussian beam beta = 1, sigma_z = 5 mm, 3x3 wake taps active.
 
-A "step" is one leapfrog step of the whole grid (prologue with the wake taps, H pass,
-E pass with the beam current), replayed from CUDA graphs with the step number on the
-device -- the loop wakesolve runs.  Inputs are far larger than L2 (22 GB per step), so
-no L2 flush is needed between steps.
+A "step" is one leapfrog step of the whole grid (prologue with the wake taps, then the
+fused step -- or the H and E passes -- with the beam current), replayed from CUDA graphs
+with the step number on the device: the loop wakesolve runs.  Inputs are far larger
+than L2 (14 GB per step with coded coefficients, 22 GB dense), so no L2 flush is needed
+between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line.  value = Mcell-updates/s (cells x steps / device time) with the
 fields resident in HBM; e2e = the same metric for a complete wakesolve through the
 public API (host geometry in, wake potential and impedance out, every host<->device
-copy inside the timed region); roofline = the E pass (the dominant kernel) timed live
-with CUDA events against the measured HBM copy bandwidth; cpu_baseline = the CPU
+copy inside the timed region); roofline = the dominant kernel (the fused step; the E
+pass when the two-pass kernels run) timed live with CUDA events against the measured
+HBM copy bandwidth, on the bytes it moves; cpu_baseline = the CPU
 oracle (scipy sparse operator, the reference's algorithm) on a bounded slab of the
 same workload.
 """
@@ -329,7 +331,7 @@ def run_ours(args, rank, world):
            "config": {"workload": f"cfg4 pillbox {P.nx}x{P.ny}x{P.nz} FP32, sigma=5.8e7 walls (relaxation form), "
                                   f"16-cell z PML, beam sigma_z=5 mm, 3x3 wake taps",
                       "cells": N, "run_steps": Nt, "cfln": P.cfln, "dt": float(s.dt),
-                      "l2": "no flush: inputs (22 GB per step) far larger than the 129 MB L2",
+                      "l2": "no flush: inputs (14 GB per step coded, 22 GB dense) far larger than the 129 MB L2",
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "roofline": {"bound": "hbm", "kernel": "k_epass%s (E pass, lossy, FP32)" % ("_coded" if coded else ""),
                         "achieved": ach_e, "peak": peak, "unit": "GB/s", "frac": ach_e / peak, "traffic": traffic,
