@@ -309,3 +309,34 @@ CONFIGS = {
         source=dict(type="WavePacket", zs=13, sigmaz=0.3, sigmaxy=100.0, wavelength=0.2, amplitude=1.0),
         Nt=2000, probes=64),
 }
+
+
+# ----------------------------------------------------------------------------- Ez files
+# WakeSolver post-processing of a recorded Ez line history (no solver run): seeded
+# synthetic histories with the reference's Ez.h5 keys, non-uniform dz, FP32-valued slabs.
+WAKE_FILE_CASES = {
+    "wakefile_3d": dict(seed=21, nz=40, nt=320, t0=0.0, shape3=True, plane="both",
+                        wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=1.0, skip_cells=0)),
+    # skip_cells trims z; t0 > 0 makes early taps' time index negative (wraps in the reference)
+    "wakefile_3d_skip_t0": dict(seed=22, nz=40, nt=320, t0=12e-12, shape3=True, plane="both",
+                                wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=1.0, skip_cells=2)),
+    # beta 0.8, a history too short for the late taps, longitudinal from 1-D slabs
+    "wakefile_long_1d": dict(seed=23, nz=40, nt=200, t0=0.0, shape3=False, plane="longitudinal",
+                             wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=0.8, skip_cells=0)),
+}
+
+
+def synthetic_history(seed, nz=40, nt=320, shape3=True, t0=0.0):
+    """(meta, slabs): meta holds the x, y, z, dx, dy, dz, t datasets of an Ez file; slabs
+    (nt, 3, 3, nz) or (nt, nz) float64 holding FP32 values."""
+    rng = np.random.default_rng(seed)
+    dz = 1e-3 * (0.8 + 0.4 * rng.random(nz))
+    zedges = np.concatenate([[-0.02], -0.02 + np.cumsum(dz)])
+    z = 0.5 * (zedges[1:] + zedges[:-1])
+    dt = 0.45 * dz.min() / 299792458.0
+    t = t0 + np.arange(0, nt * dt, dt)[:nt]
+    x = np.array([-1.1e-3, 0.0, 0.9e-3])
+    y = np.array([-0.8e-3, 0.0, 1.2e-3])
+    shape = (nt, 3, 3, nz) if shape3 else (nt, nz)
+    slabs = rng.standard_normal(shape).astype(np.float32).astype(np.float64) * 1e3
+    return dict(x=x, y=y, z=z, dx=np.full(3, 1e-3), dy=np.full(3, 1e-3), dz=dz, t=t), slabs

@@ -145,6 +145,26 @@ def run_userloop(wakis, name, case, out):
     out[name] = dict(dt=np.float64(solver.dt), E=solver.E.toarray(), H=solver.H.toarray(), J=solver.J.toarray())
 
 
+def run_wakefile(wakis, name, case, out):
+    """The reference's WakeSolver post-processing of a synthetic Ez file (written through
+    the h5py stand-in), without a solver run."""
+    import h5py  # the stand-in
+    meta, slabs = C.synthetic_history(case["seed"], case["nz"], case["nt"], case["shape3"], case["t0"])
+    fname = os.path.join(os.getcwd(), name + "_Ez.h5")
+    hf = h5py.File(fname, "w")
+    for k, v in meta.items():
+        hf[k] = v
+    for n in range(len(slabs)):
+        hf["#" + str(n).zfill(5)] = slabs[n]
+    wake = wakis.WakeSolver(save=False, verbose=0, Ez_file=fname, **case["wake"])
+    wake.solve(compute_plane=case["plane"])
+    res = dict(s=wake.s, WP=wake.WP, f=wake.f, Z=wake.Z, lambdas=wake.lambdas,
+               slab_sum=np.float64(np.sum(slabs)))
+    if case["plane"] != "longitudinal":
+        res.update(WP_3d=wake.WP_3d, WPx=wake.WPx, WPy=wake.WPy, Zx=wake.Zx, Zy=wake.Zy)
+    out[name] = res
+
+
 def test001_inputs(ref_root):
     """Golden vectors held by the reference's tests/test_001_pec_cubic_cavity.py, plus the
     STL bounds (the domain) parsed from tests/stl/001_cubic_cavity.stl."""
@@ -199,6 +219,11 @@ def main():
                 print("case", name, flush=True)
                 {"wake": run_wake, "emsolve": run_emsolve, "resonator": run_resonator,
                  "userloop": run_userloop}[case["kind"]](wakis, name, case, out)
+            for name, case in C.WAKE_FILE_CASES.items():
+                if a.only and name != a.only:
+                    continue
+                print("case", name, flush=True)
+                run_wakefile(wakis, name, case, out)
             if a.test001:
                 inp = test001_inputs(ref_root)
                 res = run_test001(wakis, inp)

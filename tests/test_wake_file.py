@@ -10,8 +10,9 @@ import pytest
 import torch
 from scipy.constants import c as c_light
 
+import cases as C
 from oracle import fit_oracle as O
-from oracle_runner import rel_l2
+from oracle_runner import load_golden, rel_l2
 
 gpu = pytest.mark.gpu
 
@@ -183,3 +184,53 @@ def test_wp_index_equals_oracle_table():
         assert nt == nt2 and nz == it2.shape[1]
         np.testing.assert_array_equal(np.where(it < 0, it + nt, it)[valid2], it2[valid2])
         np.testing.assert_array_equal(it < nt, valid2)
+
+
+# ---------------------------------------------------------------- pinned to the reference
+# tests/golden/wakefile_*.npz: the reference's own WakeSolver.solve() on the seeded
+# synthetic Ez files of cases.WAKE_FILE_CASES (tests/golden/make_golden.py)
+
+def _file_case(name, tmp_path):
+    case = C.WAKE_FILE_CASES[name]
+    meta, slabs = C.synthetic_history(case["seed"], case["nz"], case["nt"], case["shape3"], case["t0"])
+    ref = load_golden(name)
+    assert float(ref["slab_sum"]) == float(np.sum(slabs))  # the generator did not drift
+    return case, meta, slabs, ref
+
+
+@pytest.mark.parametrize("name", list(C.WAKE_FILE_CASES))
+def test_oracle_file_post_processing_matches_reference(name, tmp_path):
+    case, meta, slabs, ref = _file_case(name, tmp_path)
+    ow = oracle_wake(meta, slabs, case["plane"], **case["wake"])
+    np.testing.assert_array_equal(ow.s, ref["s"])
+    np.testing.assert_array_equal(ow.WP, ref["WP"])
+    np.testing.assert_array_equal(ow.f, ref["f"])
+    assert rel_l2(ow.Z, ref["Z"]) < 1e-12
+    if case["plane"] != "longitudinal":
+        np.testing.assert_array_equal(ow.WP_3d, ref["WP_3d"])
+        for k in ("WPx", "WPy", "Zx", "Zy"):
+            assert rel_l2(getattr(ow, k), ref[k]) < 1e-12, k
+
+
+@gpu
+@pytest.mark.parametrize("name", list(C.WAKE_FILE_CASES))
+def test_solve_from_file_matches_reference(name, tmp_path):
+    """The device path against the reference's own post-processing of the same file:
+    s, WP and WP_3d bit for bit; the transverse wake (prefix sums) and the impedances
+    (DFT against numpy's FFT) to FP64 rounding."""
+    need_gpu()
+    import wakis_gb300 as wg
+    case, meta, slabs, ref = _file_case(name, tmp_path)
+    fname = write_file(tmp_path / "Ez.npz", meta, slabs)
+    w = wg.WakeSolver(save=False, verbose=0, Ez_file=fname, **case["wake"])
+    w.solve(compute_plane=case["plane"])
+    np.testing.assert_array_equal(w.s, ref["s"])
+    np.testing.assert_array_equal(w.WP, ref["WP"])
+    np.testing.assert_array_equal(w.f, ref["f"])
+    assert rel_l2(w.Z, ref["Z"]) < 1e-10
+    if case["plane"] != "longitudinal":
+        np.testing.assert_array_equal(w.WP_3d, ref["WP_3d"])
+        for k in ("WPx", "WPy"):
+            assert rel_l2(getattr(w, k), ref[k]) < 1e-12, k
+        for k in ("Zx", "Zy"):
+            assert rel_l2(getattr(w, k), ref[k]) < 1e-10, k
