@@ -214,6 +214,43 @@ def cpu_sample_rate(nz_slab=16, steps=20, budget_s=25.0, barrier=None):
 
 
 # ----------------------------------------------------------------------------- runs
+def run_cpu_configs(args):
+    """The CPU oracle (scipy CSR leapfrog, the reference's algorithm, one thread) on the
+    config 0, 1 and 2 grids in FP64 and FP32: Mcell-updates/s over --cpu-steps steps after
+    one warm-up step (random fields), and the config-0 time-to-impedance (its whole
+    FP64 wakesolve, set-up included).  Prints one JSON line."""
+    for p in (os.path.join(ROOT, "tests"), os.path.join(ROOT, "tests", "golden")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    import cases as C
+    from oracle_runner import oracle_solver, run_oracle_case
+    rates = {}
+    for name in ("config0", "config1a", "config2"):
+        for dt in ("float64", "float32"):
+            t0 = time.perf_counter()
+            s = oracle_solver(dict(C.CONFIGS[name], dtype=dt))
+            setup = time.perf_counter() - t0
+            rng = np.random.default_rng(0)
+            s.E[:] = rng.standard_normal(s.E.size).astype(s.E.dtype)
+            s.one_step()
+            t0 = time.perf_counter()
+            for _ in range(args.cpu_steps):
+                s.one_step()
+            sec = time.perf_counter() - t0
+            rates[f"{name}_{dt}"] = {"cells": int(s.N), "steps": args.cpu_steps, "seconds": sec,
+                                     "mcell_updates_per_s": s.N * args.cpu_steps / sec / 1e6,
+                                     "operator_setup_s": setup}
+            del s
+    t0 = time.perf_counter()
+    r = run_oracle_case("config0", case=C.CONFIGS["config0"])
+    tti = time.perf_counter() - t0
+    print(json.dumps({"mode": "cpu_configs", "impl": "oracle (scipy CSR, one thread)", "threads": 1,
+                      "host_cpus": os.cpu_count(), "rates": rates,
+                      "config0_time_to_impedance": {"seconds": tti, "steps": int(r["Nt"]),
+                                                    "what": "FP64 wakesolve of config 0 through the oracle, "
+                                                            "grid and operator set-up included"}}), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -668,6 +705,9 @@ def main():
     ap.add_argument("--serve-no-saturated", action="store_true")
     ap.add_argument("--fused-shape", type=int, nargs=4, default=None, metavar=("VEC", "ROWS", "ZSEG", "CTAS"),
                     help="fused step tile shape (skips the autotuner)")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="CPU oracle rates on configs 0-2 (FP64, FP32) and the config-0 time-to-impedance")
+    ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--dense", action="store_true", help="fused step with dense coefficient arrays (no codes)")
     ap.add_argument("--variant", default="auto", choices=["auto", "staged", "direct", "fused"],
                     help="step kernels: auto (the solver default: fused where it applies), direct H/E pass kernels, "
@@ -678,7 +718,9 @@ def main():
     if world > 1 and args.impl == "ours":
         import torch
         torch.distributed.init_process_group("nccl")
-    if args.serve:
+    if args.cpu_configs:
+        run_cpu_configs(args)
+    elif args.serve:
         run_serve(args)
     elif args.accuracy or args.accuracy_cfg4:
         run_accuracy(args)
