@@ -234,3 +234,37 @@ def test_solve_from_file_matches_reference(name, tmp_path):
             assert rel_l2(getattr(w, k), ref[k]) < 1e-12, k
         for k in ("Zx", "Zy"):
             assert rel_l2(getattr(w, k), ref[k]) < 1e-10, k
+
+
+def test_text_results_round_trip(tmp_path):
+    """save_txt / read_txt / load_results follow the reference's file formats
+    (wakis/wakeSolver.py:1366-1511): header keys with units, complex columns, lambda.txt."""
+    import wakis_gb300 as wg
+    w = wg.WakeSolver(save=True, verbose=0, results_folder=str(tmp_path), **WAKE)
+    rng = np.random.default_rng(8)
+    s = np.linspace(-0.01, 0.02, 50)
+    f = np.linspace(0.0, 5e9, 40)
+    cols = dict(WP=rng.standard_normal(50), WPx=rng.standard_normal(50), WPy=rng.standard_normal(50),
+                lambdas=rng.random(50), Z=rng.standard_normal(40) + 1j * rng.standard_normal(40),
+                Zx=rng.standard_normal(40) + 1j * rng.standard_normal(40),
+                Zy=rng.standard_normal(40) + 1j * rng.standard_normal(40),
+                lambdaf=rng.standard_normal(40) + 1j * rng.standard_normal(40))
+    w._savetxt("WP.txt", s, cols["WP"], "WP [V/pC]", "   s [m]")
+    w._savetxt("WPx.txt", s, cols["WPx"], "WP [V/pC]", "   s [m]")
+    w._savetxt("WPy.txt", s, cols["WPy"], "WP [V/pC]", "   s [m]")
+    w._savetxt("lambda.txt", s, cols["lambdas"], "Charge distribution [C/m]", "   s [Hz]")
+    w._savetxt("Z.txt", -f, cols["Z"], "Z [Ohm]", "   f [Hz]")
+    w._savetxt("spectrum.txt", f, cols["lambdaf"], "Charge distribution spectrum [C/s]", "   f [Hz]")
+    w._savetxt("Zx.txt", f, cols["Zx"], "Zx [Ohm]", "   f [Hz]")
+    w._savetxt("Zy.txt", f, cols["Zy"], "Zy [Ohm]", "   f [Hz]")
+    d = w.read_txt(str(tmp_path / "WP.txt"))
+    assert list(d) == ["s[m]", "WP[V/pC]"]
+    w2 = wg.WakeSolver(save=False, verbose=0, **WAKE)
+    w2.load_results(str(tmp_path))
+    np.testing.assert_allclose(w2.s, s, rtol=1e-15)
+    np.testing.assert_allclose(w2.f, f, rtol=1e-15)  # abs() of the stored column
+    for k, v in cols.items():
+        np.testing.assert_allclose(np.asarray(getattr(w2, k)), v, rtol=1e-15, err_msg=k)
+    assert w2.wakelength == w2.s[-1] and w2.Ez_file.endswith("/Ez.h5")
+    w.save_txt(str(tmp_path / "extra.txt"), s, cols["WP"], x_name="s [m]", y_name="WP [V/pC]")
+    assert list(w.read_txt(str(tmp_path / "extra.txt"))) == ["s[m]", "WP[V/pC]"]

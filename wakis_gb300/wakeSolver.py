@@ -353,12 +353,16 @@ class WakeSolver:
             else:
                 raise ValueError("Dimension error: check input dimensions")
         self.lambdas = np.interp(self.s, z, chargedist / self.q)
+        if self.save:
+            self._savetxt("lambda.txt", self.s, self.lambdas, "Charge distribution [C/m]", "   s [Hz]")
 
     def calc_lambdas_analytic(self, **kwargs):
         """Gaussian lambda(s) (wakis/wakeSolver.py:842-874)."""
         for key, val in kwargs.items():
             setattr(self, key, val)
         self.lambdas = 1 / (self.sigmaz * np.sqrt(2 * np.pi)) * np.exp(-(self.s ** 2) / (2 * self.sigmaz ** 2))
+        if self.save:  # the reference labels this file's s column "[Hz]"
+            self._savetxt("lambda.txt", self.s, self.lambdas, "Charge distribution [C/m]", "   s [Hz]")
 
     # ------------------------------------------------------------------ utilities
     @staticmethod
@@ -430,19 +434,60 @@ class WakeSolver:
             return hf
 
     def read_txt(self, txt, skiprows=2, delimiter=None, usecols=None):
+        """Columns of a text result file as a dict (wakis/wakeSolver.py:1366-1420): keys are
+        the header's column names with their units ("s[m]", "WP[V/pC]"), or 0, 1, ...
+        when the file has no such header; complex columns are read as complex128."""
         try:
             load = np.loadtxt(txt, skiprows=skiprows, delimiter=delimiter, usecols=usecols)
         except Exception:
+            self.log(f"[!] Using dtype=np.complex128 to read {txt}", level=2)
             load = np.loadtxt(txt, skiprows=skiprows, delimiter=delimiter, usecols=usecols, dtype=np.complex128)
         try:
             with open(txt) as f:
-                header = f.readline().split()
+                header = f.readline()
+            header = header.replace(" ", "").replace("#", "").replace("\n", "").split("]")
+            d = {}
+            for i in range(len(load[0, :])):
+                d[header[i] + "]"] = load[:, i]
         except Exception:
-            header = []
-        d = {}
-        for i in range(load.shape[1]):
-            d[header[i] if i < len(header) else i] = load[:, i]
+            self.log("[!] Using integer keys since no header was found", level=2)
+            d = {}
+            for i in range(len(load[0, :])):
+                d[i] = load[:, i]
         return d
+
+    def save_txt(self, f_name, x_data=None, y_data=None, x_name="X [-]", y_name="Y [-]"):
+        """Two-column text file f_name(.txt) with the reference's header
+        (wakis/wakeSolver.py:1422-1475)."""
+        if f_name.endswith(".txt"):
+            f_name = f_name[:-4]
+        if x_data is not None and y_data is not None:
+            np.savetxt(f_name + ".txt", np.c_[x_data, y_data], header="   " + x_name + " " * 20 + y_name + "\n" + "-" * 48)
+        else:
+            self.log("[!] txt not saved, please provide x_data and y_data")
+
+    def load_results(self, folder=None):
+        """Reads the results a run with save=True wrote (wakis/wakeSolver.py:1477-1511):
+        lambdas, WPx, WPy, s, WP, lambdaf, Zx, Zy, f (absolute value) and Z; sets
+        wakelength = s[-1], folder and Ez_file = folder + 'Ez.h5'."""
+        if folder is None and self.folder is None:
+            raise Exception("[!] Please provide a folder path")
+        elif folder is None:
+            folder = self.folder
+        if not folder.endswith("/"):
+            folder = folder + "/"
+        _, self.lambdas = self.read_txt(folder + "lambda.txt").values()
+        _, self.WPx = self.read_txt(folder + "WPx.txt").values()
+        _, self.WPy = self.read_txt(folder + "WPy.txt").values()
+        self.s, self.WP = self.read_txt(folder + "WP.txt").values()
+        _, self.lambdaf = self.read_txt(folder + "spectrum.txt").values()
+        _, self.Zx = self.read_txt(folder + "Zx.txt").values()
+        _, self.Zy = self.read_txt(folder + "Zy.txt").values()
+        self.f, self.Z = self.read_txt(folder + "Z.txt").values()
+        self.f = np.abs(self.f)
+        self.wakelength = self.s[-1]
+        self.folder = folder
+        self.Ez_file = folder + "Ez.h5"
 
     def _savetxt(self, name, a, b, label, xlabel):
         np.savetxt(self.folder + name, np.c_[a, b], header=xlabel + " " * 20 + label + "\n" + "-" * 48)
