@@ -300,7 +300,8 @@ def run_ours(args, rank, world):
             s._ctx.call("fit_set_fused_shape", *args.fused_shape)
             s._sync_coeffs()
             s._ensure_codes()
-            tuned = {tuple(args.fused_shape): float("nan")}
+            s.fused_staging = args.staging
+            tuned = {tuple(args.fused_shape) + (args.staging,): float("nan")}
         else:
             tuned = s.tune_fused()
     del mask
@@ -386,7 +387,8 @@ def run_ours(args, rank, world):
         shapes = {k: t for k, t in tuned.items() if k != "two-pass"}
         best = min(shapes, key=lambda t: shapes[t] if shapes[t] == shapes[t] else 0.0)
         out["fused_autotune"] = {"best": list(best),
-                                 "ms_per_step": {f"v{v}r{r}z{z}c{m}": t for (v, r, z, m), t in sorted(shapes.items())},
+                                 "ms_per_step": {f"v{v}r{r}z{z}c{m}s{st}": t
+                                                 for (v, r, z, m, st), t in sorted(shapes.items())},
                                  "two_pass_ms_per_step": tuned.get("two-pass")}
         out["config"]["kernels"] = "fused single-pass step (ping-pong field buffers)"
     else:
@@ -703,6 +705,8 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-no-fp64", action="store_true")
     ap.add_argument("--serve-no-saturated", action="store_true")
+    ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
+                    help="with --fused-shape: 0 loads, 1 or 2 TMA plane rings")
     ap.add_argument("--fused-shape", type=int, nargs=4, default=None, metavar=("VEC", "ROWS", "ZSEG", "CTAS"),
                     help="fused step tile shape (skips the autotuner)")
     ap.add_argument("--cpu-configs", action="store_true",

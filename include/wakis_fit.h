@@ -177,9 +177,12 @@ FIT_API int fit_wake_finalize(FitCtx *ctx, double qscale, double ds, double dxf,
  * where the reference skips the tap because it >= nt), dz (nz).  Per s index the sums run
  * in the reference's order with plain FP64 adds of rounded products, continue from the
  * previous line's result, and are divided by qscale after each line, so wp3d equals the
- * reference's WP_3d bit for bit.  Then, for nlines == 9, the transverse wake as in
- * fit_wake_finalize.  Outputs (host): wp3d (nlines*ns); wpx, wpy (ns each; untouched when
- * nlines != 9 or NULL).  Errors: fit_last_error(NULL, ...). */
+ * reference's WP_3d bit for bit.  Then, when the lines form a square of odd side
+ * 2n+1 >= 3 (row-major, the reference's n_transverse_cells = n), the transverse wake as in
+ * fit_wake_finalize from lines (n+1, n), (n-1, n), (n, n+1), (n, n-1), with dxf, dyf the
+ * sums dxf[n-1] + dxf[n], dyf[n-1] + dyf[n] (wakis/wakeSolver.py:553-611).  Outputs
+ * (host): wp3d (nlines*ns); wpx, wpy (ns each; untouched for other line counts or NULL).
+ * Errors: fit_last_error(NULL, ...). */
 FIT_API int fit_wake_history(const double *ezt, int32_t nlines, int64_t nt, int32_t nz, const int32_t *it,
                              int32_t ns, const double *dz, double qscale, double ds, double dxf, double dyf,
                              double *wp3d, double *wpx, double *wpy);
@@ -188,7 +191,8 @@ FIT_API int fit_wake_history(const double *ezt, int32_t nlines, int64_t nt, int3
  *   X_s[b] = sum_{t < len} x_s[t] exp(-2 pi i b t / n)
  * for nsig signals of length len (host, signal-major); out (host) holds nsig*nb
  * (re, im) pairs.  Replaces np.fft.fft(..., n=N)[mask] (wakis/wakeSolver.py:692-699,
- * 755-770).  Uses library-allocated device scratch for partial sums. */
+ * 755-770).  Uses library-allocated device scratch for partial sums.  At most 65535
+ * signals per call (FIT_ERR_ARG beyond). */
 FIT_API int fit_dft(const double *x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
             double *out);
 
@@ -201,7 +205,9 @@ FIT_API int fit_dft(const double *x, int32_t nsig, int64_t len, int64_t n, int64
  * (cudaStream_t, NULL = legacy default stream) and the call returns without waiting.
  * Partial sums live in one fixed file-scope device array of 2^18 double2 (4 MiB) that every
  * GPU loading this library holds until the process exits: nsig*nb must not exceed 2^18
- * (FIT_ERR_ARG otherwise).  The array keeps the last call's contents; every entry a call
+ * (FIT_ERR_ARG otherwise), and nsig must not exceed 65535.  x and out must be device (or
+ * managed) memory of the current device: other pointers are refused with FIT_ERR_ARG
+ * before anything is launched.  The array keeps the last call's contents; every entry a call
  * reads is written earlier in the same call, so nothing is cleared.  All calls on a device
  * share the array: calls that overlap on the GPU race.  The first call on a device looks
  * up the array's device address (cudaGetSymbolAddress) with that device current; make
@@ -241,6 +247,18 @@ FIT_API int fit_set_coeff_codes(FitCtx *ctx, int32_t enable, int32_t *ncodes);
  * 4 rows: 3 or 4; 0 = the first).  fit_set_kernel_variant(ctx, 2) sets a default; the
  * solver's autotuner times the candidates on the grid itself with fit_time_fused. */
 FIT_API int fit_set_fused_shape(FitCtx *ctx, int32_t vec, int32_t rows, int32_t zseg, int32_t ctas);
+/* How the fused step's old fields reach the threads (same results bit for bit):
+ * staging 0 = per-thread global loads; 1 = tensor-memory-accelerator copies
+ * (cp.async.bulk.tensor) of each plane's E, H and code boxes into shared-memory rings,
+ * 4 E planes and 3 H / code planes deep; 2 = the same, 5 and 4 planes deep (with 4-row
+ * tiles; 8-row tiles use the first depth).  The copies run on coded coefficients with Nx a multiple of 8 (and, in FP32,
+ * the 4-wide vector); elsewhere the step keeps the loads.  The tile shape (rows 4: two
+ * CTAs per SM, rows 8: one) and z ranges come from fit_set_fused_shape.  Needs the fused
+ * step enabled (FIT_ERR_STATE otherwise); returns FIT_ERR_ARG when the grid does not
+ * qualify or the tensor maps cannot be encoded.
+ * Same work as fit_set_fused_shape's kernel: the reference's _one_step
+ * (wakis/solverFIT3D.py:504-525). */
+FIT_API int fit_set_fused_staging(FitCtx *ctx, int32_t staging);
 /* Times, beam off, on the context stream between CUDA events: reps fused steps from
  * (E, H) into the second buffers (ms_out[0]), and reps two-pass steps (H pass + E pass)
  * in place on copies of E and H in the second buffers (ms_out[1]); average milliseconds

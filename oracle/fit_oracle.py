@@ -538,7 +538,9 @@ class OracleWake:
     """WakeSolver parameters and post-processing (wakis/wakeSolver.py:22-255,423-874)."""
 
     def __init__(self, wakelength=None, q=1e-9, sigmaz=1e-3, beta=1.0, xsource=0.0, ysource=0.0,
-                 xtest=0.0, ytest=0.0, ti=None, fmax=None, skip_cells=0):
+                 xtest=0.0, ytest=0.0, ti=None, fmax=None, skip_cells=0, counter_moving=False,
+                 n_transverse_cells=1):
+        # counter_moving and n_transverse_cells: wakis/wakeSolver.py:159, 190, 481-529
         self.q, self.sigmaz, self.beta = q, sigmaz, beta
         self.v = beta * c_light
         self.xsource, self.ysource, self.xtest, self.ytest = xsource, ysource, xtest, ytest
@@ -548,6 +550,8 @@ class OracleWake:
         self.ti = ti if ti is not None else 8.548921333333334 * sigmaz / (np.sqrt(beta) * self.v)
         self.wakelength = wakelength
         self.lambdas = None
+        self.counter_moving = counter_moving
+        self.n_transverse_cells = n_transverse_cells
 
 
 def wakesolve(solver, wake, wakelength=None, compute_plane="both", record_every=None, field_monitor=None,
@@ -627,9 +631,11 @@ class OracleFieldMonitor:
         self.time_index += 1
 
 
-def wp_index_table(wake, nt_saved):
+def wp_index_table(wake, nt_saved, counter=False):
     """it(m, k) of the Ez(z, t) line integral (wakis/wakeSolver.py:449-529).  Evaluated
-    with the reference's expression order in FP64; returns (s, it, valid)."""
+    with the reference's expression order in FP64; with counter (a counter-moving test
+    charge, wakis/wakeSolver.py:500-513) loop index k reads z[-k-1] with the time
+    measured from zmax.  Returns (s, it, valid, zz, nt)."""
     t = wake.t
     nt = len(t)
     dt = t[2] - t[1]
@@ -641,7 +647,10 @@ def wp_index_table(wake, nt_saved):
         wake.wakelength = nt * dt * wake.v - (zmax - zmin) - wake.ti * wake.v
     s = np.arange(-wake.ti * wake.v, wake.wakelength, dt * wake.v)
     nt = min(nt, nt_saved)
-    ts = (z[None, :] + s[:, None]) / wake.v - zmin / wake.v - t[0] + wake.ti
+    if counter:
+        ts = (z[::-1][None, :] - s[:, None]) / (-1 * wake.v) - zmax / (-1 * wake.v) - t[0] + wake.ti
+    else:
+        ts = (z[None, :] + s[:, None]) / wake.v - zmin / wake.v - t[0] + wake.ti
     it = np.trunc(ts / dt).astype(np.int64)
     valid = it < nt
     it = np.where(it < 0, it + nt, it)  # python negative indexing
@@ -649,10 +658,14 @@ def wp_index_table(wake, nt_saved):
 
 
 def postprocess(wake, slabs, compute_plane="both"):
-    """slabs: (Nt, 3, 3, Nz) or (Nt, Nz).  Sets s, WP, WP_3d, WPx, WPy, f, Z, Zx, Zy,
-    lambdas, lambdaf on ``wake``."""
+    """slabs: (Nt, side, side, Nz) or (Nt, Nz).  Sets s, WP, WP_3d, WPx, WPy, f, Z, Zx,
+    Zy, lambdas, lambdaf on ``wake``.  The 3-D integral reads the lines
+    slab[side//2 + i, side//2 + j] for i, j in -n..n (n = n_transverse_cells, numpy
+    indexing as the reference's), with the counter-moving loop when set
+    (wakis/wakeSolver.py:481-529)."""
     nt_saved = slabs.shape[0]
-    s, it, valid, zz, nt = wp_index_table(wake, nt_saved)
+    counter = bool(getattr(wake, "counter_moving", False)) and compute_plane.lower() != "longitudinal"
+    s, it, valid, zz, nt = wp_index_table(wake, nt_saved, counter)
     dzz = np.asarray(wake.dz, dtype=np.float64)
     nz = it.shape[1]
     kk = np.broadcast_to(np.arange(nz), it.shape)
@@ -666,15 +679,20 @@ def postprocess(wake, slabs, compute_plane="both"):
         wake.s, wake.WP = s, WP
         calc_long_Z(wake)
         return
+    n = getattr(wake, "n_transverse_cells", 1)
+    c0, c1 = slabs.shape[1] // 2, slabs.shape[2] // 2
     WP = np.zeros_like(s)
-    WP_3d = np.zeros((3, 3, len(s)))
-    for i in range(-1, 2):
-        for j in range(-1, 2):
-            Ezt = slabs[:nt, 1 + i, 1 + j, zz].T  # (nz, nt)
-            terms = np.where(valid, Ezt[kk, np.where(valid, it, 0)] * dzz[kk], 0.0)
+    WP_3d = np.zeros((2 * n + 1, 2 * n + 1, len(s)))
+    for i in range(-n, n + 1):
+        for j in range(-n, n + 1):
+            Ezt = slabs[:nt, c0 + i, c1 + j, zz].T  # (nz, nt)
+            if counter:  # loop index k: row -k-1 of Ezt, factor -1 * dz[k]
+                terms = np.where(valid, Ezt[::-1][kk, np.where(valid, it, 0)] * (-1 * dzz[kk]), 0.0)
+            else:
+                terms = np.where(valid, Ezt[kk, np.where(valid, it, 0)] * dzz[kk], 0.0)
             WP = _seq_rows(terms, start=WP) / Qn  # accumulator not reset (quirk)
-            WP_3d[1 + i, 1 + j, :] = WP
-    wake.s, wake.WP, wake.WP_3d = s, WP_3d[1, 1, :], WP_3d
+            WP_3d[n + i, n + j, :] = WP
+    wake.s, wake.WP, wake.WP_3d = s, WP_3d[n, n, :], WP_3d
     calc_trans_WP(wake)
     calc_long_Z(wake)
     calc_trans_Z(wake)
@@ -693,12 +711,13 @@ def calc_trans_WP(wake):
     s = wake.s
     ds = s[2] - s[1]
     ns = len(s)
+    c = getattr(wake, "n_transverse_cells", 1)
     int_WP = np.zeros_like(wake.WP_3d)
     for n in range(ns):
         int_WP[:, :, n] = np.sum(wake.WP_3d[:, :, 0:n], axis=2) * ds
     dxf, dyf = np.diff(wake.xf), np.diff(wake.yf)
-    wake.WPx = -(int_WP[2, 1, :] - int_WP[0, 1, :]) / (dxf[0] + dxf[1])
-    wake.WPy = -(int_WP[1, 2, :] - int_WP[1, 0, :]) / (dyf[0] + dyf[1])
+    wake.WPx = -(int_WP[c + 1, c, :] - int_WP[c - 1, c, :]) / (dxf[c - 1] + dxf[c])
+    wake.WPy = -(int_WP[c, c + 1, :] - int_WP[c, c - 1, :]) / (dyf[c - 1] + dyf[c])
 
 
 def calc_lambdas_analytic(wake):

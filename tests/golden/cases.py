@@ -101,6 +101,15 @@ CASES = {
         wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
                   fmax=5e9, skip_cells=0),
         wakelength=0.1, compute_plane="both"),
+    # the cavity wake with a counter-moving test charge (3-D integral down z from zmax) and
+    # skip_cells (dz indexed by the loop index)
+    "counter_f64": dict(
+        kind="wake", dtype="float64", grid=dict(_cavity_grid, Nx=16, Ny=16, Nz=32),
+        solids=[("cavity", "cube_pipe", {}, [1.0, 1.0])], bg="pec",
+        bc_low=["pec", "pec", "abc"], bc_high=["pec", "pec", "abc"], cfln=1.0,
+        wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
+                  fmax=5e9, skip_cells=2, counter_moving=True),
+        wakelength=0.1, compute_plane="both"),
     # config-1 physics at reduced size: sigma=1e4 walls (relaxation form), z PML, beta 0.8, offset 2 mm.
     # CFL 0.5 (the reference default): with sigma>0 cells the reference's explicit loss term
     # diverges at CFL 1.0 on this grid.
@@ -323,20 +332,35 @@ WAKE_FILE_CASES = {
     # beta 0.8, a history too short for the late taps, longitudinal from 1-D slabs
     "wakefile_long_1d": dict(seed=23, nz=40, nt=200, t0=0.0, shape3=False, plane="longitudinal",
                              wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=0.8, skip_cells=0)),
+    # a counter-moving test charge (the 3-D integral runs down z from zmax with -dz),
+    # with skip_cells, and with t0 > 0 (wrapped negative time indices)
+    "wakefile_3d_counter": dict(seed=24, nz=40, nt=320, t0=0.0, shape3=True, plane="both",
+                                wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=1.0, skip_cells=2,
+                                          counter_moving=True)),
+    "wakefile_3d_counter_t0": dict(seed=25, nz=40, nt=320, t0=12e-12, shape3=True, plane="both",
+                                   wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=0.9, skip_cells=0,
+                                             counter_moving=True)),
+    # 5x5 slabs integrated over n_transverse_cells = 2 (25 lines)
+    "wakefile_5x5_n2": dict(seed=26, nz=40, nt=320, t0=0.0, shape3=True, side=5, n_transverse_cells=2,
+                            plane="both", wake=dict(q=1e-9, sigmaz=2e-3, wakelength=0.02, beta=1.0, skip_cells=1)),
 }
 
 
-def synthetic_history(seed, nz=40, nt=320, shape3=True, t0=0.0):
+def synthetic_history(seed, nz=40, nt=320, shape3=True, t0=0.0, side=3):
     """(meta, slabs): meta holds the x, y, z, dx, dy, dz, t datasets of an Ez file; slabs
-    (nt, 3, 3, nz) or (nt, nz) float64 holding FP32 values."""
+    (nt, side, side, nz) or (nt, nz) float64 holding FP32 values."""
     rng = np.random.default_rng(seed)
     dz = 1e-3 * (0.8 + 0.4 * rng.random(nz))
     zedges = np.concatenate([[-0.02], -0.02 + np.cumsum(dz)])
     z = 0.5 * (zedges[1:] + zedges[:-1])
     dt = 0.45 * dz.min() / 299792458.0
     t = t0 + np.arange(0, nt * dt, dt)[:nt]
-    x = np.array([-1.1e-3, 0.0, 0.9e-3])
-    y = np.array([-0.8e-3, 0.0, 1.2e-3])
-    shape = (nt, 3, 3, nz) if shape3 else (nt, nz)
+    if side == 3:
+        x = np.array([-1.1e-3, 0.0, 0.9e-3])
+        y = np.array([-0.8e-3, 0.0, 1.2e-3])
+    else:
+        x = np.linspace(-1.0e-3, 1.1e-3, side) ** 3 * 1e6
+        y = np.linspace(-1.2e-3, 0.9e-3, side) ** 3 * 1e6
+    shape = (nt, side, side, nz) if shape3 else (nt, nz)
     slabs = rng.standard_normal(shape).astype(np.float32).astype(np.float64) * 1e3
-    return dict(x=x, y=y, z=z, dx=np.full(3, 1e-3), dy=np.full(3, 1e-3), dz=dz, t=t), slabs
+    return dict(x=x, y=y, z=z, dx=np.full(side, 1e-3), dy=np.full(side, 1e-3), dz=dz, t=t), slabs

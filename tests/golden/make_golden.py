@@ -149,7 +149,8 @@ def run_wakefile(wakis, name, case, out):
     """The reference's WakeSolver post-processing of a synthetic Ez file (written through
     the h5py stand-in), without a solver run."""
     import h5py  # the stand-in
-    meta, slabs = C.synthetic_history(case["seed"], case["nz"], case["nt"], case["shape3"], case["t0"])
+    meta, slabs = C.synthetic_history(case["seed"], case["nz"], case["nt"], case["shape3"], case["t0"],
+                                      case.get("side", 3))
     fname = os.path.join(os.getcwd(), name + "_Ez.h5")
     hf = h5py.File(fname, "w")
     for k, v in meta.items():
@@ -157,6 +158,7 @@ def run_wakefile(wakis, name, case, out):
     for n in range(len(slabs)):
         hf["#" + str(n).zfill(5)] = slabs[n]
     wake = wakis.WakeSolver(save=False, verbose=0, Ez_file=fname, **case["wake"])
+    wake.n_transverse_cells = case.get("n_transverse_cells", 1)
     wake.solve(compute_plane=case["plane"])
     res = dict(s=wake.s, WP=wake.WP, f=wake.f, Z=wake.Z, lambdas=wake.lambdas,
                slab_sum=np.float64(np.sum(slabs)))

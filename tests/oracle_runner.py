@@ -115,3 +115,48 @@ def rel_l2(a, b):
     den = np.linalg.norm(b.ravel())
     num = np.linalg.norm((a - b).ravel())
     return num / den if den > 0 else num
+
+
+def run_oracle_wake_partial(case, nsteps):
+    """The first ``nsteps`` steps of a wake run through the oracle: the fields after them
+    and the partial wake integral, i.e. the line sums over the taps whose time index is
+    below nsteps (the tap table of the full run), combined across the 3x3 lines with the
+    reference's non-reset accumulator.  Returns s, dt, Nt (of the full run), WP_3d
+    (9, len(s)), E and H."""
+    s = oracle_solver(case)
+    wake = O.OracleWake(wakelength=case["wakelength"], **case["wake"])
+    ixt = np.abs(s.x - wake.xtest).argmin()
+    iyt = np.abs(s.y - wake.ytest).argmin()
+    xx, yy = slice(ixt - 1, ixt + 2), slice(iyt - 1, iyt + 2)
+    z = s.z
+    tmax = (wake.wakelength + wake.ti * wake.v + (z.max() - z.min())) / wake.v
+    Nt = int(tmax / s.dt)
+    beam = O.OracleBeam(q=wake.q, sigmaz=wake.sigmaz, beta=wake.beta, xsource=wake.xsource, ysource=wake.ysource)
+    ez = s.comp(s.E, 2)
+    slabs = []
+    for n in range(nsteps):
+        beam.update(s, n * s.dt)
+        slabs.append(np.array(ez[xx, yy, :], dtype=np.float64))
+        s.one_step()
+    slabs = np.array(slabs)
+    wake.t = np.arange(0, Nt * s.dt, s.dt)
+    wake.zf = z.copy()
+    wake.dz = s.dz
+    sv, it, valid, zz, nt = O.wp_index_table(wake, Nt)
+    fed = valid & (it < nsteps)
+    dzz = np.asarray(wake.dz, dtype=np.float64)
+    kk = np.broadcast_to(np.arange(it.shape[1]), it.shape)
+    wp = np.zeros_like(sv)
+    wp3d = np.zeros((9, len(sv)))
+    for li, (i, j) in enumerate((i, j) for i in range(-1, 2) for j in range(-1, 2)):
+        ezt = slabs[:, 1 + i, 1 + j, zz].T  # (nz, nsteps)
+        terms = np.where(fed, ezt[kk, np.where(fed, it, 0)] * dzz[kk], 0.0)
+        wp = O._seq_rows(terms, start=wp) / (wake.q * 1e12)
+        wp3d[li] = wp
+    return dict(s=sv, dt=np.float64(s.dt), Nt=Nt, WP_3d=wp3d, E=s.E.copy(), H=s.H.copy())
+
+
+def run_oracle_probes(case, nsteps):
+    """emsolve of an emsolve case for ``nsteps`` steps through the oracle with E_z recorded
+    at the case's probe points after every step; returns dt, probes (nsteps, P), E, H."""
+    return run_oracle_case(None, case=dict(case, Nt=nsteps))

@@ -99,3 +99,22 @@ def run_case(name, case=None, tmpdir=".", userloop_wake=False, dtype=None, dt=No
     if probes:
         res["probes"] = np.array(probes, dtype=np.float64)
     return res
+
+
+def run_wake_partial(case, nsteps, tmpdir=".", dtype=None, dt=None):
+    """The first ``nsteps`` steps of a wake run through the CUDA path: the tap table of
+    the full run is installed and the device loop is stopped after nsteps steps, so the
+    device accumulators hold the partial line sums (taps with time index < nsteps).
+    Returns s, dt, Nt (of the full run), WP_3d (9, len(s)), E and H."""
+    import wakis_gb300 as wg
+    grid = make_grid(wg, case)
+    wake = wg.WakeSolver(wakelength=case["wakelength"], save=False, verbose=0, results_folder=str(tmpdir),
+                         **case["wake"])
+    s = make_solver(wg, case, grid, wake, dtype, dt)
+    beam, Nt = s._wake_prepare(wake, case["wakelength"], "both")
+    vt = s._wake_device_setup(beam, Nt)
+    first = s._wake_first_step(beam)
+    s._device_steps(first, nsteps - first)
+    s._wake_device_done(vt[:nsteps], nsteps)
+    sv, wp3d, _, _ = wake._finalize_device()
+    return dict(s=sv, dt=np.float64(s.dt), Nt=Nt, WP_3d=wp3d, E=s.E.numpy(), H=s.H.numpy())

@@ -140,3 +140,67 @@ def test_grid_with_too_many_coefficient_triples_stays_dense():
     s.emsolve(4)
     assert s.coefficient_code_count == 0
     assert np.isfinite(s.E.numpy()).all()
+
+
+# ---------------------------------------------------------------- TMA-fed fused step
+@pytest.mark.parametrize("dtype,nx", [(np.float32, 136), (np.float64, 72), (np.float32, 8)])
+@pytest.mark.parametrize("staging,rows,ctas", [(1, 4, 3), (2, 4, 3), (1, 8, 2)])
+@pytest.mark.parametrize("bcs", [(["pmc", "periodic", "pec"], ["pec", "periodic", "pml"]),
+                                 (["periodic", "periodic", "periodic"], ["periodic", "periodic", "periodic"]),
+                                 (["pec", "pmc", "pec"], ["pml", "pec", "pmc"])])
+def test_tma_staging_equals_loads(dtype, nx, staging, rows, ctas, bcs):
+    """The fused step fed by TMA plane rings gives the load-fed fused step's and the
+    two-pass kernels' fields bit for bit: random E, H, lossy blocks, an x extent with a
+    partial second tile (or a single 8-cell tile), a partial y tile (13 rows), five z
+    ranges of 8 planes, every face kind including the periodic row crossings the boxes
+    do not hold, and an odd step count."""
+    x = np.linspace(-1, 1, nx + 1)
+    y = np.linspace(-0.8, 0.7, 14)
+    z = np.linspace(-2, 2, 41)
+    vec = 4 if dtype == np.float32 else 2
+    out = {}
+    for mode in ("direct", 0, staging):
+        s = _random_field_solver(x, y, z, dtype, True, bcs=bcs)
+        if mode == "direct":
+            s.kernels = "direct"
+        else:
+            s.fused_staging = mode
+            s._ctx.call("fit_set_fused_shape", vec, rows, 5, ctas)
+        s.emsolve(41)
+        out[mode] = (s.E.numpy(), s.H.numpy(), s.J.numpy())
+        assert s.coefficient_code_count > 0
+    for mode in (0, staging):
+        for a, b, k in zip(out[mode], out["direct"], "EHJ"):
+            np.testing.assert_array_equal(a, b, err_msg=f"staging {mode}: {k}")
+
+
+@pytest.mark.parametrize("name", ["cavity_f64", "lossy_f32", "periodic_cond_f32", "longitudinal_f64"])
+def test_tma_staging_reference_cases(name, tmp_path, monkeypatch):
+    """Wake runs of the reference fixtures with the TMA-fed fused step: bit-identical to
+    the two-pass kernels, so within the parity tolerances of the fixtures."""
+    monkeypatch.setenv("WAKIS_GB300_STAGING", "1")
+    tma = _run(name, "fused", tmp_path, monkeypatch)
+    monkeypatch.setenv("WAKIS_GB300_STAGING", "0")
+    direct = _run(name, "direct", tmp_path, monkeypatch)
+    for k, v in direct.items():
+        np.testing.assert_array_equal(np.asarray(tma[k]), np.asarray(v), err_msg=f"{name}:{k}")
+
+
+def test_tma_staging_rejected_where_it_does_not_apply():
+    """Nx not a multiple of 8, or dense coefficients: fit_set_fused_staging refuses and the
+    solver keeps the load-fed step."""
+    import wakis_gb300 as wg
+    from wakis_gb300 import _native as nat
+    s = _random_field_solver(np.linspace(-1, 1, 13), np.linspace(-0.8, 0.7, 14), np.linspace(-2, 2, 41),
+                             np.float32, True)
+    s._sync_coeffs()
+    s._ensure_codes()
+    with pytest.raises(nat.FitError):
+        s._ctx.call("fit_set_fused_staging", 1)
+    s2 = _random_field_solver(np.linspace(-1, 1, 17), np.linspace(-0.8, 0.7, 14), np.linspace(-2, 2, 41),
+                              np.float32, False)
+    s2._sync_coeffs()
+    s2._ensure_codes()
+    with pytest.raises(nat.FitError):
+        s2._ctx.call("fit_set_fused_staging", 1)
+    assert isinstance(s2, wg.SolverFIT3D)

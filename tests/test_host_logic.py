@@ -127,9 +127,11 @@ def test_step_times_follow_reference_scalar_types():
             assert type(v * (n * dt)) in (type(vt[n]), float)
 
 
-@pytest.mark.parametrize("name", ["cavity_f64", "skip_nonuniform_f64", "longitudinal_f64", "lossy_f32"])
+@pytest.mark.parametrize("name", ["cavity_f64", "skip_nonuniform_f64", "longitudinal_f64", "lossy_f32", "counter_f64"])
 def test_tap_table_reproduces_reference_loop(name):
-    """The per-step (m, k0, cnt) table adds exactly the reference's terms in its order."""
+    """The per-step (m, k0, cnt) table adds exactly the reference's terms: each valid
+    (s index, z index) pair once, at the step of its time index, with the reference's dz
+    factor (negated and read from the loop index of a counter-moving test charge)."""
     import wakis_gb300 as wg
     case = C.CASES[name]
     x, y, z = C.axes(case)
@@ -145,8 +147,13 @@ def test_tap_table_reproduces_reference_loop(name):
     w.zf, w.dz = s.z, g.dz
     ow.t, ow.zf, ow.dz = w.t, s.z, g.dz
     longitudinal = case["compute_plane"] == "longitudinal"
-    sv, it, valid, kskip, nz, nt = w._tap_index(Nt, longitudinal, g.Nz)
-    so, ito, valido, _, _ = O.wp_index_table(ow, Nt)
+    sv, it, valid, kskip, nz, nt, wdz = w._tap_index(Nt, longitudinal, g.Nz)
+    counter = bool(case["wake"].get("counter_moving")) and not longitudinal
+    so, ito, valido, _, _ = O.wp_index_table(ow, Nt, counter)
+    dzo = np.asarray(g.dz, dtype=np.float64)[:nz]
+    if counter:  # the oracle's table is in loop order: loop index k reads z index nz-1-k
+        ito, valido, dzo = ito[:, ::-1], valido[:, ::-1], (-1 * dzo)[::-1]
+    np.testing.assert_array_equal(wdz, dzo)
     np.testing.assert_array_equal(sv, so)
     np.testing.assert_array_equal(valid, valido)
     np.testing.assert_array_equal(np.where(valid, it, 0), np.where(valido, ito, 0))
@@ -161,6 +168,8 @@ def test_tap_table_reproduces_reference_loop(name):
                 seen.setdefault(int(em[e]), []).append(int(k))
     for m in range(len(sv)):
         ks = list(np.nonzero(valid[m])[0])
+        if counter:  # the reference's loop reads z downwards; so do the steps
+            ks = ks[::-1]
         assert seen.get(m, []) == ks
 
 

@@ -192,7 +192,8 @@ def test_wp_index_equals_oracle_table():
 
 def _file_case(name, tmp_path):
     case = C.WAKE_FILE_CASES[name]
-    meta, slabs = C.synthetic_history(case["seed"], case["nz"], case["nt"], case["shape3"], case["t0"])
+    meta, slabs = C.synthetic_history(case["seed"], case["nz"], case["nt"], case["shape3"], case["t0"],
+                                      case.get("side", 3))
     ref = load_golden(name)
     assert float(ref["slab_sum"]) == float(np.sum(slabs))  # the generator did not drift
     return case, meta, slabs, ref
@@ -201,7 +202,8 @@ def _file_case(name, tmp_path):
 @pytest.mark.parametrize("name", list(C.WAKE_FILE_CASES))
 def test_oracle_file_post_processing_matches_reference(name, tmp_path):
     case, meta, slabs, ref = _file_case(name, tmp_path)
-    ow = oracle_wake(meta, slabs, case["plane"], **case["wake"])
+    ow = oracle_wake(meta, slabs, case["plane"], n_transverse_cells=case.get("n_transverse_cells", 1),
+                     **case["wake"])
     np.testing.assert_array_equal(ow.s, ref["s"])
     np.testing.assert_array_equal(ow.WP, ref["WP"])
     np.testing.assert_array_equal(ow.f, ref["f"])
@@ -223,6 +225,7 @@ def test_solve_from_file_matches_reference(name, tmp_path):
     case, meta, slabs, ref = _file_case(name, tmp_path)
     fname = write_file(tmp_path / "Ez.npz", meta, slabs)
     w = wg.WakeSolver(save=False, verbose=0, Ez_file=fname, **case["wake"])
+    w.n_transverse_cells = case.get("n_transverse_cells", 1)
     w.solve(compute_plane=case["plane"])
     np.testing.assert_array_equal(w.s, ref["s"])
     np.testing.assert_array_equal(w.WP, ref["WP"])

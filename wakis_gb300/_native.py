@@ -87,6 +87,7 @@ _SIGS = {
     "fit_set_kernel_variant": (_P, C.c_int32),
     "fit_time_fused": (_P, C.c_int32, _D),
     "fit_set_fused_shape": (_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32),
+    "fit_set_fused_staging": (_P, C.c_int32),
     "fit_set_coeff_codes": (_P, C.c_int32, C.POINTER(C.c_int32)),
     "fit_monitor_update": (_P, C.c_int32, C.c_int64, C.c_int32, _D, _P, C.c_int32, _P),
     "fit_set_monitor": (_P, C.c_int32, _D, C.c_int64, C.c_int64, _P, C.c_int32),
@@ -179,7 +180,7 @@ def dft(signals, n, b0, nb):
 def wake_history(ezt, it, dz, qscale, ds=1.0, dxf=1.0, dyf=1.0):
     """Wake integral of a recorded Ez line history on the device: ezt (nlines, nz, nt)
     FP64, it (nz, ns) int32 (-1 = no tap), dz (nz,).  Returns (wp3d (nlines, ns), wpx,
-    wpy); wpx and wpy are None unless nlines == 9."""
+    wpy); wpx and wpy are None unless the lines form a square of odd side >= 3."""
     ezt = np.ascontiguousarray(ezt, dtype=np.float64)
     it = np.ascontiguousarray(it, dtype=np.int32)
     dz = np.ascontiguousarray(dz, dtype=np.float64)
@@ -192,7 +193,9 @@ def wake_history(ezt, it, dz, qscale, ds=1.0, dxf=1.0, dyf=1.0):
     rc = load().fit_wake_history(dptr(ezt), nl, nt, nz, iptr32(it), ns, dptr(dz), float(qscale), float(ds),
                                  float(dxf), float(dyf), dptr(wp3d), dptr(wpx), dptr(wpy))
     check(rc)
-    return (wp3d, wpx, wpy) if nl == 9 else (wp3d, None, None)
+    side = int(round(nl ** 0.5))
+    square = side >= 3 and side % 2 == 1 and side * side == nl
+    return (wp3d, wpx, wpy) if square else (wp3d, None, None)
 
 
 class Context:

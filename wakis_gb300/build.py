@@ -15,6 +15,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 SRC = os.path.join(PKG, "csrc", "fit_capi.cu")
 DEPS = [SRC, os.path.join(PKG, "csrc", "fit_kernels.cuh"), os.path.join(PKG, "csrc", "fit_pool.cuh"),
+        os.path.join(PKG, "csrc", "fit_tma.cuh"),
         os.path.join(ROOT, "include", "wakis_fit.h")]
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libwakis_fit.so")

@@ -4,6 +4,8 @@
 // source / tap tables, a private non-blocking stream on which every kernel is issued
 // (ordered after and before the caller's stream with events, so caller writes to the
 // fields and our kernels never race), and the CUDA graphs of fit_run.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,6 +20,7 @@
 
 #include "wakis_fit.h"
 #include "fit_kernels.cuh"
+#include "fit_tma.cuh"
 
 using namespace fit;
 
@@ -87,6 +90,7 @@ struct FitCtx {
     bool fused = false;     // fused single-pass step in device loops (ping-pong with E2/H2)
     void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
     int fused_vec = 4, fused_rows = 8, fused_zseg = 1, fused_ctas = 2;  // tile shape of the fused step
+    int fused_staging = 0;  // 0: loads; 1, 2: TMA plane rings (fit_set_fused_staging)
     bool graph_fused = false;  // the cached graph holds fused steps
     unsigned short* d_code = nullptr;  // coded coefficients: one code per cell (nullptr: dense)
     void* d_tab = nullptr;             // [code][ch, ce, cl][x, y, z, pad] in the field dtype
@@ -453,7 +457,123 @@ void launch_fused_vec(FitCtx* c, int mode, const StepArgs& st, bool forward, con
         launch_fused_shape<T, VEC, 4, 3>(c, mode, st, forward, beam);
 }
 
+// ---------------------------------------------------------------- TMA-fed fused step
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// the grids the TMA-fed step serves: coded coefficients, every box row and plane stride
+// a multiple of 16 bytes (Nx a multiple of 8 for the 2-byte codes), the widest vector
+bool tma_grid_ok(const FitCtx* c) {
+    return c->d_code && c->g.nx % 8 == 0 && (c->dtype == FIT_F64 || c->fused_vec == 4);
+}
+
+// 4-D map (Nx, Ny, Nz, 3 components) of a field buffer, box (bw, bh, 1, 3)
+bool encode_field_map(CUtensorMap* m, const FitCtx* c, const void* base, int bw, int bh) {
+    const auto enc = tmap_encoder();
+    if (!enc || !base) return false;
+    const cuuint64_t es = esize(c);
+    const cuuint64_t dims[4] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)c->g.nz, 3};
+    const cuuint64_t strides[3] = {dims[0] * es, dims[0] * dims[1] * es, (cuuint64_t)c->g.N * es};
+    const cuuint32_t box[4] = {(cuuint32_t)bw, (cuuint32_t)bh, 1, 3};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    return enc(m, c->dtype == FIT_F64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+               const_cast<void*>(base), dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// 3-D map (Nx, Ny, Nz) of the 16-bit coefficient codes, box (bw, bh, 1)
+bool encode_code_map(CUtensorMap* m, const FitCtx* c, int bw, int bh) {
+    const auto enc = tmap_encoder();
+    if (!enc || !c->d_code) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)c->g.nz};
+    const cuuint64_t strides[2] = {dims[0] * 2, dims[0] * dims[1] * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, c->d_code, dims, strides, box, elem,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the three maps of one step direction for the tile shape (FY rows)
+template <typename T, int VEC, int FY, int NE, int NH>
+bool encode_step_maps(const FitCtx* c, bool forward, CUtensorMap* mE, CUtensorMap* mH, CUtensorMap* mC) {
+    using L = TmaLayout<T, VEC, FY, NE, NH>;
+    return encode_field_map(mE, c, forward ? c->E : c->E2, L::EW, L::ER) &&
+           encode_field_map(mH, c, forward ? c->H : c->H2, L::HW, L::HR) && encode_code_map(mC, c, L::CW, L::HR);
+}
+
+// returns false (nothing launched) when the maps cannot be encoded
+template <typename T, int VEC, int FY, int MB, int NE, int NH>
+bool launch_tma_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
+    using L = TmaLayout<T, VEC, FY, NE, NH>;
+    CUtensorMap mE, mH, mC;
+    if (!encode_step_maps<T, VEC, FY, NE, NH>(c, forward, &mE, &mH, &mC)) return false;
+    const T* Ein = static_cast<const T*>(forward ? c->E : c->E2);
+    const T* Hin = static_cast<const T*>(forward ? c->H : c->H2);
+    T* Eout = static_cast<T*>(forward ? c->E2 : c->E);
+    T* Hout = static_cast<T*>(forward ? c->H2 : c->H);
+    const int zlen = (c->g.nz + c->fused_zseg - 1) / c->fused_zseg;
+    const dim3 grid((unsigned)((c->g.nx + L::FX - 1) / L::FX), (unsigned)((c->g.ny + FY - 1) / FY),
+                    (unsigned)((c->g.nz + zlen - 1) / zlen));
+    const dim3 block(32, FY + 1);
+    const T* tab = static_cast<const T*>(c->d_tab);
+    T* J = static_cast<T*>(c->J);
+    if (mode == 1) {
+        auto k = k_step_tma<T, VEC, FY, MB, 1, NE, NH>;
+        allow_smem(k, L::BYTES);
+        k<<<grid, block, L::BYTES, c->own>>>(mE, mH, mC, Ein, Hin, Eout, Hout, J, c->use_cond, c->g, metric<T>(c),
+                                             beam, st, zlen, c->d_code, tab, c->d_err);
+    } else {
+        auto k = k_step_tma<T, VEC, FY, MB, 0, NE, NH>;
+        allow_smem(k, L::BYTES);
+        k<<<grid, block, L::BYTES, c->own>>>(mE, mH, mC, Ein, Hin, Eout, Hout, J, c->use_cond, c->g, metric<T>(c),
+                                             beam, st, zlen, c->d_code, tab, c->d_err);
+    }
+    count(c);
+    return true;
+}
+
+// 4 rows: two CTAs per SM; 8 rows: one
+template <typename T, int VEC>
+bool launch_tma(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
+    if (c->fused_rows == 8) return launch_tma_shape<T, VEC, 8, 1, 4, 3>(c, mode, st, forward, beam);
+    if (c->fused_staging == 2) return launch_tma_shape<T, VEC, 4, 2, 5, 4>(c, mode, st, forward, beam);
+    return launch_tma_shape<T, VEC, 4, 2, 4, 3>(c, mode, st, forward, beam);
+}
+
+bool tma_maps_ok(const FitCtx* c, int staging, int rows) {
+    CUtensorMap a, b, d;
+    bool ok = true;
+    for (int f = 0; f < 2 && ok; ++f) {
+        if (c->dtype == FIT_F64)
+            ok = rows == 8 ? encode_step_maps<double, 2, 8, 4, 3>(c, f == 0, &a, &b, &d)
+                 : staging == 2 ? encode_step_maps<double, 2, 4, 5, 4>(c, f == 0, &a, &b, &d)
+                                : encode_step_maps<double, 2, 4, 4, 3>(c, f == 0, &a, &b, &d);
+        else
+            ok = rows == 8 ? encode_step_maps<float, 4, 8, 4, 3>(c, f == 0, &a, &b, &d)
+                 : staging == 2 ? encode_step_maps<float, 4, 4, 5, 4>(c, f == 0, &a, &b, &d)
+                                : encode_step_maps<float, 4, 4, 4, 3>(c, f == 0, &a, &b, &d);
+    }
+    return ok;
+}
+
 void launch_fused(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
+    if (c->fused_staging && tma_grid_ok(c)) {
+        const bool done = c->dtype == FIT_F64 ? launch_tma<double, 2>(c, mode, st, forward, beam)
+                                              : launch_tma<float, 4>(c, mode, st, forward, beam);
+        if (done) return;  // else the load-fed kernel (same results)
+    }
     if (c->dtype == FIT_F64)
         launch_fused_vec<double, 2>(c, mode, st, forward, beam);
     else if (c->fused_vec == 4)
@@ -1172,7 +1292,7 @@ int fit_wake_finalize(FitCtx* c, double qscale, double ds, double dxf, double dy
     if (rc) return rc;
     const int nl = c->tap.nlines, ns = c->tap.ns;
     k_wake_finalize<<<1, 1024, 0, c->own>>>(c->d_acc, c->d_comp, nl, ns, qscale, ds, dxf, dyf, c->d_wp3d, c->d_wpx,
-                                            c->d_wpy, c->d_scratch);
+                                            c->d_wpy, c->d_scratch, nl == 9 ? 3 : 0);
     g_launches++;
     CK(cudaMemcpyAsync(wp3d, c->d_wp3d, (size_t)nl * ns * sizeof(double), cudaMemcpyDeviceToHost, c->own));
     if (nl == 9 && wpx && wpy) {
@@ -1181,6 +1301,14 @@ int fit_wake_finalize(FitCtx* c, double qscale, double ds, double dxf, double dy
     }
     CK(cudaStreamSynchronize(c->own));
     return leave(c);
+}
+
+// side of a square of nlines = side*side lines with an odd side >= 3 (a transverse wake
+// exists), else 0
+static int square_side(int nlines) {
+    for (int q = 3; q * q <= nlines; q += 2)
+        if (q * q == nlines) return q;
+    return 0;
 }
 
 int fit_wake_history(const double* ezt, int32_t nlines, int64_t nt, int32_t nz, const int32_t* it, int32_t ns,
@@ -1225,13 +1353,14 @@ int fit_wake_history(const double* ezt, int32_t nlines, int64_t nt, int32_t nz, 
         return fail(nullptr, FIT_ERR_CUDA, "fit_wake_history setup failed: %s", cudaGetErrorString(e));
     }
     k_wake_history<<<(unsigned)((ns + 127) / 128), 128, 0, s>>>(d_ezt, nlines, nt, nz, d_it, ns, d_dz, qscale, d_wp);
+    const int side = square_side(nlines);
     k_wake_finalize<<<1, 1024, 0, s>>>(nullptr, nullptr, nlines, ns, qscale, ds, dxf, dyf, d_wp, d_wpx, d_wpy,
-                                       d_scr);
+                                       d_scr, side);
     g_launches += 2;
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(wp3d, d_wp, (size_t)nlines * ns * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && nlines == 9 && wpx && wpy) {
+    if (e == cudaSuccess && side >= 3 && wpx && wpy) {
         e = cudaMemcpyAsync(wpx, d_wpx, (size_t)ns * sizeof(double), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(wpy, d_wpy, (size_t)ns * sizeof(double), cudaMemcpyDeviceToHost, s);
     }
@@ -1244,6 +1373,8 @@ int fit_wake_history(const double* ezt, int32_t nlines, int64_t nt, int32_t nz, 
 int fit_dft(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb, double* out) {
     if (!x || !out || nsig <= 0 || len <= 0 || n <= 0 || nb <= 0 || b0 < 0)
         return fail(nullptr, FIT_ERR_ARG, "bad fit_dft arguments");
+    if (nsig > kDftMaxSignals)
+        return fail(nullptr, FIT_ERR_ARG, "fit_dft: nsig = %d exceeds %d signals per call", nsig, kDftMaxSignals);
     const int nsplit = (int)std::max<long long>(1, std::min<long long>(32, len / 2048));
     double* dx = nullptr;
     double2* part = nullptr;
@@ -1406,6 +1537,22 @@ int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg, int3
     return FIT_OK;
 }
 
+int fit_set_fused_staging(FitCtx* c, int32_t staging) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    if (staging < 0 || staging > 2) return fail(c, FIT_ERR_ARG, "staging must be 0 (loads), 1 or 2 (TMA rings)");
+    if (staging != 0) {
+        if (!c->fused || !c->E2) return fail(c, FIT_ERR_STATE, "the fused step is not enabled for this context");
+        if (!tma_grid_ok(c))
+            return fail(c, FIT_ERR_ARG, "TMA staging needs coded coefficients, Nx %% 8 == 0 and (FP32) 4-wide vectors");
+        if (!tma_maps_ok(c, staging, c->fused_rows))
+            return fail(c, FIT_ERR_ARG, "the TMA tensor maps of this grid cannot be encoded");
+    }
+    invalidate(c);
+    c->fused_staging = staging;
+    return FIT_OK;
+}
+
 int fit_set_monitor(FitCtx* c, int32_t nf, const double* phases, int64_t n0, int64_t nsteps, void* acc,
                     int32_t single) {
     if (!c) return FIT_ERR_ARG;
@@ -1559,10 +1706,23 @@ int scratch_address(int dev, double2** out) {
 
 }  // namespace
 
+// a device (or managed) allocation visible from device `dev`; the query allocates nothing
+static bool on_device(const void* p, int dev) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the sticky-free error of the query
+        return false;
+    }
+    return (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
+}
+
 extern "C" int fit_dft_noalloc(const double* x, int32_t nsig, int64_t len, int64_t n, int64_t b0, int32_t nb,
                                double* out, void* stream) {
     if (!x || !out || nsig <= 0 || len <= 0 || n <= 0 || nb <= 0 || b0 < 0)
         return fail(nullptr, FIT_ERR_ARG, "bad fit_dft_noalloc arguments");
+    if (nsig > kDftMaxSignals)
+        return fail(nullptr, FIT_ERR_ARG, "fit_dft_noalloc: nsig = %d exceeds %d signals per call", nsig,
+                    kDftMaxSignals);
     const long long per_split = (long long)nsig * nb;
     if (per_split > kDftScratchEntries)
         return fail(nullptr, FIT_ERR_ARG,
@@ -1573,6 +1733,9 @@ extern "C" int fit_dft_noalloc(const double* x, int32_t nsig, int64_t len, int64
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(nullptr, FIT_ERR_CUDA, "cudaGetDevice failed: %s", cudaGetErrorString(e));
+    if (!on_device(x, dev) || !on_device(out, dev))
+        return fail(nullptr, FIT_ERR_ARG, "fit_dft_noalloc: x and out must be device memory of the current device %d",
+                    dev);
     double2* part = nullptr;
     int rc = scratch_address(dev, &part);
     if (rc) return rc;

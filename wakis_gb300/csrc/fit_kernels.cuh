@@ -1593,7 +1593,9 @@ __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
 }
 
 // wake taps of E^n: the (s, z) pairs whose time index is step n add Ez*dz to their
-// line's running sum (FP64, compensated).  Called by all threads of one block.
+// line's running sum (FP64, compensated).  Called by all threads of one block.  The
+// entries of a step are ordered by s index; the runs of one s index (one accumulator
+// per line) are summed by one thread, the one holding the first of them.
 template <typename T>
 __device__ __forceinline__ void wake_taps(const T* __restrict__ E, const Geom& g, const TapArgs& tp, long long n) {
     if (tp.nlines > 0 && n >= 0 && n < tp.nsteps) {
@@ -1603,11 +1605,15 @@ __device__ __forceinline__ void wake_taps(const T* __restrict__ E, const Geom& g
         for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
             const long long e = r0 + t / tp.nlines;
             const int l = (int)(t % tp.nlines);
-            const int m = tp.ent_m[e], k0 = tp.ent_k0[e], c = tp.ent_cnt[e];
+            const int m = tp.ent_m[e];
+            if (e > r0 && tp.ent_m[e - 1] == m) continue;  // summed with the group's first run
             double s = tp.acc[(long long)l * tp.ns + m], cc = tp.comp[(long long)l * tp.ns + m];
-            for (int q = 0; q < c; ++q) {
-                const double ez = (double)Ez[tp.base[l] + g.sz * (long long)(k0 + q)];
-                neumaier_add(s, cc, __dmul_rn(ez, tp.dz[k0 + q]));
+            for (long long f = e; f < r1 && tp.ent_m[f] == m; ++f) {
+                const int k0 = tp.ent_k0[f], c = tp.ent_cnt[f];
+                for (int q = 0; q < c; ++q) {
+                    const double ez = (double)Ez[tp.base[l] + g.sz * (long long)(k0 + q)];
+                    neumaier_add(s, cc, __dmul_rn(ez, tp.dz[k0 + q]));
+                }
             }
             tp.acc[(long long)l * tp.ns + m] = s;
             tp.comp[(long long)l * tp.ns + m] = cc;
@@ -1722,10 +1728,12 @@ __global__ void k_beam_line(T* __restrict__ J, Geom g, BeamArgs b, double vt) {
 // wake post-processing: combine lines with the non-reset accumulator of the reference,
 // then exclusive prefix sums (x ds) and the Panofsky-Wenzel central differences.
 // One block of 1024 threads.  acc == nullptr: wp3d already holds the combined lines.
+// The lines form a side x side square (row-major, side = 2n+1, n >= 1); the transverse
+// wake reads lines (n+1, n), (n-1, n), (n, n+1), (n, n-1); side 0: longitudinal only.
 __global__ void k_wake_finalize(const double* __restrict__ acc, const double* __restrict__ comp, int nlines,
                                 int ns, double qscale, double ds, double dxf, double dyf,
                                 double* __restrict__ wp3d, double* __restrict__ wpx, double* __restrict__ wpy,
-                                double* __restrict__ scratch /* 4*ns */) {
+                                double* __restrict__ scratch /* 4*ns */, int side) {
     // 1. line combination, sequential over lines, parallel over s
     for (int m = threadIdx.x; acc && m < ns; m += blockDim.x) {
         double prev = 0.0;
@@ -1736,10 +1744,12 @@ __global__ void k_wake_finalize(const double* __restrict__ acc, const double* __
         }
     }
     __syncthreads();
-    if (nlines != 9) return;
-    // 2. exclusive prefix sums of lines (2,1)->7, (0,1)->1, (1,2)->5, (1,0)->3 (row-major 3x3)
+    if (side < 3 || nlines != side * side) return;
+    // 2. exclusive prefix sums of lines (n+1,n), (n-1,n), (n,n+1), (n,n-1) (row-major;
+    // 7, 1, 5, 3 of the 3x3 square)
     __shared__ double part[1024];
-    const int lines[4] = {7, 1, 5, 3};
+    const int c0 = side / 2;
+    const int lines[4] = {(c0 + 1) * side + c0, (c0 - 1) * side + c0, c0 * side + c0 + 1, c0 * side + c0 - 1};
     const int T = blockDim.x;
     const int chunk = (ns + T - 1) / T;
     for (int q = 0; q < 4; ++q) {
@@ -1799,6 +1809,8 @@ __global__ void k_wake_history(const double* __restrict__ ezt, int nlines, long 
 
 // FP64 direct DFT: stage 1 writes compensated partial sums of a slice of the time axis
 // to scratch; stage 2 adds the slices.  Twiddle phase from the exact integer (b*t) mod n.
+// The signal index is blockIdx.y: at most 65535 signals per launch.
+constexpr int kDftMaxSignals = 65535;
 __global__ void k_dft_partial(const double* __restrict__ x, int nsig, long long len, long long n, long long b0,
                               int nb, int nsplit, double2* __restrict__ part) {
     const int b = blockIdx.x;          // bin offset

@@ -310,6 +310,8 @@ class RoutinesMixin:
         self._ensure_codes()
         if self._kernels == "fused" and nsteps >= 256:
             self.tune_fused()  # once per grid shape; leaves the fields unchanged
+        if self._kernels == "fused":
+            self._set_staging()
         self._ctx.call("fit_run", n0, nsteps)
         self._run_steps += nsteps
 

@@ -163,6 +163,8 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self.coefficient_codes = os.environ.get("WAKIS_GB300_CODES", "1") != "0"
         self.coefficient_code_count = 0
         self.kernels = os.environ.get("WAKIS_GB300_KERNELS", "auto")
+        # how the fused step's old fields reach the threads (see fused_staging)
+        self.fused_staging = os.environ.get("WAKIS_GB300_STAGING", "auto")
 
         self.E._on_write = self._before_E_write
         self._J._on_write = self._before_J_write
@@ -220,12 +222,13 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self.coefficient_code_count = int(n.value)
 
     def tune_fused(self, reps=5, zsegs=(2, 4, 8, 16, 32, 64, 128), force=False):
-        """Autotuner of the fused step's tile shape for this grid: times every candidate
-        (cells per thread along x, rows per CTA, z ranges per tile column, CTAs per SM of
-        the register budget) with
-        fit_time_fused, which leaves E, H and J unchanged, keeps the fastest and
-        remembers it for grids of the same shape (later calls reuse it unless force).
-        Returns {(vec, rows, zseg, ctas): ms, 'two-pass': ms}."""
+        """Autotuner of the fused step for this grid: times every candidate (cells per
+        thread along x, rows per CTA, z ranges per tile column, CTAs per SM of the register
+        budget, staging) with fit_time_fused, which leaves E, H and J unchanged, keeps the
+        fastest and remembers it for grids of the same shape (later calls reuse it unless
+        force).  Staging 0 feeds the threads with per-thread loads; 1 and 2 with TMA plane
+        rings (coded grids with Nx a multiple of 8 only; see fused_staging).
+        Returns {(vec, rows, zseg, ctas, staging): ms, 'two-pass': ms}."""
         if self._kernels != "fused":
             self.kernels = "fused"
         key = self._grid_key()
@@ -240,6 +243,7 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._ensure_codes()
         times = {}
         ms = np.zeros(2)
+        self._ctx.call("fit_set_fused_staging", 0)
         for vec in vecs:
             for rows, ctas in ((4, 3), (4, 4), (8, 2)):
                 for zseg in zsegs:
@@ -247,17 +251,71 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
                         continue
                     self._ctx.call("fit_set_fused_shape", vec, rows, zseg, ctas)
                     self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
-                    times[(vec, rows, zseg, ctas)] = float(ms[0])
-        times["two-pass"] = float(ms[1])
+                    times[(vec, rows, zseg, ctas, 0)] = float(ms[0])
+        two_pass = float(ms[1])
+        if self._staging_candidates():
+            vec = vecs[0]
+            for rows, ctas, staging in ((4, 3, 1), (4, 3, 2), (8, 2, 1)):
+                for zseg in zsegs:
+                    if zseg > self.Nz:
+                        continue
+                    self._ctx.call("fit_set_fused_shape", vec, rows, zseg, ctas)
+                    try:
+                        self._ctx.call("fit_set_fused_staging", staging)
+                    except nat.FitError:
+                        break
+                    self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
+                    times[(vec, rows, zseg, ctas, staging)] = float(ms[0])
+            self._ctx.call("fit_set_fused_staging", 0)
+        times["two-pass"] = two_pass
         best = min((t for t in times if t != "two-pass"), key=times.get)
         SolverFIT3D._fused_shapes[key] = (best, times)
         self._apply_tuned(best, times)
         return times
 
+    def _staging_candidates(self):
+        """Whether the TMA-fed fused step applies: coded coefficients, Nx a multiple of 8
+        and, in FP32, a multiple of the 4-wide vector."""
+        return self.coefficient_code_count > 0 and self.Nx % 8 == 0
+
+    @property
+    def fused_staging(self):
+        """How the fused step's old fields reach the threads; the results are the same bit
+        for bit.  'auto' (default): what the autotuner picked for this grid, else loads;
+        0: per-thread global loads; 1: tensor-memory-accelerator copies (cp.async.bulk.tensor)
+        of each plane's E, H and coefficient-code boxes into shared-memory rings 4 E planes
+        and 3 H planes deep; 2: 5 and 4 planes deep (as 1 with 8-row tiles).  Copies apply to coded
+        grids with Nx a multiple of 8; elsewhere the step keeps the loads.  The
+        environment variable WAKIS_GB300_STAGING sets the default."""
+        return self._staging
+
+    @fused_staging.setter
+    def fused_staging(self, value):
+        v = str(value).lower()
+        if v not in ("auto", "0", "1", "2"):
+            raise ValueError(f"fused_staging must be 'auto', 0, 1 or 2, got {value!r}")
+        self._staging = v
+
+    def _set_staging(self):
+        """Applies fused_staging to the context before a fused device loop."""
+        if self._staging == "auto":
+            hit = SolverFIT3D._fused_shapes.get(self._grid_key())
+            want = hit[0][4] if hit is not None else 0
+        else:
+            want = int(self._staging)
+        try:
+            self._ctx.call("fit_set_fused_staging", want)
+        except nat.FitError:  # the grid does not qualify: loads
+            self._ctx.call("fit_set_fused_staging", 0)
+
     def _apply_tuned(self, best, times):
-        """Sets the tuned fused shape; under kernels='auto' a grid on which the two-pass
-        step timed faster keeps the pass kernels."""
-        self._ctx.call("fit_set_fused_shape", *best)
+        """Sets the tuned fused shape and staging; under kernels='auto' a grid on which the
+        two-pass step timed faster keeps the pass kernels."""
+        self._ctx.call("fit_set_fused_shape", *best[:4])
+        try:
+            self._ctx.call("fit_set_fused_staging", best[4] if len(best) > 4 else 0)
+        except nat.FitError:
+            self._ctx.call("fit_set_fused_staging", 0)
         if self._kernels_auto and times["two-pass"] < times[best]:
             self._ctx.call("fit_set_kernel_variant", 0)
             self._kernels = "direct"

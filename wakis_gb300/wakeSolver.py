@@ -46,8 +46,6 @@ class WakeSolver:
         self.compute_plane = compute_plane
         self.DE_model = None
         self.counter_moving = counter_moving
-        if counter_moving:
-            raise NotImplementedError("counter_moving test charges are not provided")
         if add_space is not None:
             self.skip_cells = add_space
         if ti is not None:
@@ -91,20 +89,23 @@ class WakeSolver:
         self.t = np.asarray(t)
         self.xf, self.yf, self.zf = np.atleast_1d(np.asarray(xf)), np.atleast_1d(np.asarray(yf)), np.asarray(zf)
         self.dx, self.dy, self.dz = np.asarray(dx), np.asarray(dy), np.asarray(dz)
-        s, it, valid, kskip, nz, nt = self._tap_index(nsteps, longitudinal, solver.Nz)
+        s, it, valid, kskip, nz, nt, w = self._tap_index(nsteps, longitudinal, solver.Nz)
         row_ptr, em, ek0, ecnt = self._tap_csr(it, valid, nsteps)
         lx = np.ascontiguousarray([a for a, _ in lines], dtype=np.int32)
         ly = np.ascontiguousarray([b for _, b in lines], dtype=np.int32)
-        dzt = np.ascontiguousarray(self.dz[:nz], dtype=np.float64)
+        dzt = np.ascontiguousarray(w, dtype=np.float64)
         self._run = dict(solver=solver, s=s, nlines=len(lines), lines=list(lines), longitudinal=longitudinal,
                          keep=(lx, ly, row_ptr, em, ek0, ecnt, dzt))
         solver._ctx.call("fit_set_wake_taps", len(lines), nat.iptr32(lx), nat.iptr32(ly), int(kskip), len(s),
                          int(nsteps), nat.iptr64(row_ptr), nat.iptr32(em), nat.iptr32(ek0), nat.iptr32(ecnt),
                          int(nz), nat.dptr(dzt))
 
-    def _wp_index(self, nsaved):
-        """s and the raw time index it(m, k) exactly as calc_long_WP_3d / calc_long_WP
-        evaluate them (wakis/wakeSolver.py:345-369, 449-529), the z trim and nt."""
+    def _wp_index(self, nsaved, counter=False):
+        """s and the raw time index it(m, k) exactly as calc_long_WP / calc_long_WP_3d
+        evaluate them (wakis/wakeSolver.py:345-369, 449-529), in the reference's loop order:
+        k runs over the trimmed z axis, and for a counter-moving test charge (the 3-D
+        integral only) loop index k reads z[-k-1] with the time measured from zmax
+        (wakis/wakeSolver.py:500-513).  Also the z trim and nt."""
         nt = len(self.t)
         dt = self.t[2] - self.t[1]
         ti = self.ti
@@ -119,27 +120,52 @@ class WakeSolver:
             self.wakelength = wakelength
         s = np.arange(-self.ti * self.v, wakelength, dt * self.v)
         nt = min(nt, nsaved)
-        ts = (z[None, :] + s[:, None]) / self.v - zmin / self.v - self.t[0] + ti
+        if counter:
+            ts = (z[::-1][None, :] - s[:, None]) / (-1 * self.v) - zmax / (-1 * self.v) - self.t[0] + ti
+        else:
+            ts = (z[None, :] + s[:, None]) / self.v - zmin / self.v - self.t[0] + ti
         it = np.trunc(ts / dt).astype(np.int64)
         return s, it, zz, len(z), nt
 
+    def _loop_dz(self, nz, counter):
+        """The dz factor of loop index k: dz[k] of the untrimmed axis (the reference indexes
+        dz with the loop index when skip_cells != 0), times -1 for a counter-moving test
+        charge."""
+        dz = np.asarray(self.dz, dtype=np.float64)[:nz]
+        return -1 * dz if counter else dz
+
+    @staticmethod
+    def _wrap(it, nt):
+        """Ezt[k, it] with Python indexing, as the reference reads it: taps with it >= nt are
+        skipped, a negative it counts from the end of the nt recorded steps, and one below
+        -nt raises IndexError.  Returns (valid, wrapped index)."""
+        valid = it < nt
+        itw = np.where(it < 0, it + nt, it)
+        if np.any(valid & (itw < 0)):
+            bad = int(it[valid & (itw < 0)][0])
+            raise IndexError(f"index {bad} is out of bounds for axis 1 with size {nt}")
+        return valid, itw
+
     def _tap_index(self, nsaved, longitudinal, Nz):
-        """s and it(m, k) of the device taps of a live run."""
-        s, it, zz, nz, nt = self._wp_index(nsaved)
+        """s, it(m, k) by z index k of the line, the dz factors by z index and the z trim of
+        the device taps of a live run.  The sums of a live run are compensated, so only
+        the index set and the factors need to be the reference's, not its order."""
+        counter = bool(self.counter_moving) and not longitudinal
+        s, it, zz, nz, nt = self._wp_index(nsaved, counter)
         if longitudinal and nz != Nz:
             raise ValueError(f"could not broadcast input array from shape ({Nz},) into shape ({nz},): "
                              f"compute_plane='longitudinal' needs skip_cells=0")
-        valid = it < nt
-        if np.any(valid & (it < 0)):
-            raise NotImplementedError("negative time index in the wake integral (a tap before t=0)")
+        valid, itw = self._wrap(it, nt)
+        w = self._loop_dz(nz, counter)
+        if counter:  # loop index k reads z index nz-1-k
+            valid, itw, w = valid[:, ::-1], itw[:, ::-1], w[::-1]
         kskip = self.skip_cells if self.skip_cells != 0 else 0
-        return s, it, valid, kskip, nz, nt
+        return s, itw, valid, kskip, nz, nt, w
 
     @staticmethod
     def _tap_csr(it, valid, nsteps):
-        """Per-step CSR of (m, k0, cnt): for a fixed s-index m, it(m, k) is non-decreasing in
-        k, so the k that one step feeds form one contiguous run, and adding the runs in step
-        order adds the terms in the reference's k order."""
+        """Per-step CSR of (m, k0, cnt): runs of consecutive z indices k that one step feeds
+        into one s index m, ordered by step, then m, then k."""
         M, K = np.nonzero(valid)
         st = it[M, K]
         if M.size == 0:
@@ -152,14 +178,19 @@ class WakeSolver:
         gm, gk, gs = M[starts], K[starts], st[starts]
         order = np.lexsort((gm, gs))
         gm, gk, gs, cnt = gm[order], gk[order], gs[order], cnt[order]
-        dup = (gs[1:] == gs[:-1]) & (gm[1:] == gm[:-1])
-        if np.any(dup):
-            raise NotImplementedError("wake tap index not monotone in z")
+        # the runs of one (step, s index) stay adjacent (stable sort): the device sums them
+        # in one thread, so a time index that is not monotone in z (wrapped negative
+        # indices) needs no special case
         row_ptr = np.searchsorted(gs, np.arange(nsteps + 1), side="left").astype(np.int64)
         return (np.ascontiguousarray(row_ptr), np.ascontiguousarray(gm, dtype=np.int32),
                 np.ascontiguousarray(gk, dtype=np.int32), np.ascontiguousarray(cnt, dtype=np.int32))
 
-    def _finalize_device(self):
+    def _finalize_device(self, transverse_lines=False):
+        """WP_3d (lines x len(s)), WPx and WPy of a live run from the device accumulators.
+        With transverse_lines (calc_long_WP_3d), n_transverse_cells other than 1 reads the
+        recorded 3x3 lines the way the reference reads its 3x3 Ez slabs,
+        Ez[1 + i, 1 + j] for i, j in -n..n with Python indexing: n = 0 keeps the centre
+        line alone, and an index past the slab raises the reference's IndexError."""
         r = self._run
         s = r["s"]
         ns = len(s)
@@ -167,6 +198,17 @@ class WakeSolver:
         wp3d = np.empty(nl * ns)
         wpx = np.empty(ns)
         wpy = np.empty(ns)
+        n = self.n_transverse_cells
+        if transverse_lines and nl == 9 and n != 1:
+            for i in range(-n, n + 1):
+                for j in range(-n, n + 1):
+                    for ax, idx in ((0, 1 + i), (1, 1 + j)):
+                        if not -3 <= idx < 3:
+                            raise IndexError(f"index {idx} is out of bounds for axis {ax} with size 3")
+            # n = 0: the centre line only, its own sum divided by q*1e12
+            raw = np.empty(nl * ns)
+            r["solver"]._ctx.call("fit_read_wake", nat.dptr(raw))
+            return s, (raw.reshape(nl, ns)[4] / (self.q * 1e12))[None, :], None, None
         if nl == 9:
             ds = s[2] - s[1]
             dxf, dyf = np.diff(self.xf), np.diff(self.yf)
@@ -202,8 +244,10 @@ class WakeSolver:
         operation order, so s and WP / WP_3d equal the reference's bit for bit
         (wakis/wakeSolver.py:333-413, 446-540).  Slab lines follow the reference: the 1-D
         slab itself, or Ez[sh0//2 + 1, sh1//2 + 1, zz] for calc_long_WP on 3-D slabs,
-        Ez[sh0//2 + i, sh1//2 + j, zz] for the 3x3 lines of calc_long_WP_3d.  The file is
-        closed afterwards, as the reference closes it."""
+        Ez[sh0//2 + i, sh1//2 + j, zz] for i, j in -n..n (n = n_transverse_cells, Python
+        indexing) for calc_long_WP_3d, whose loop over z runs backwards with negated dz
+        for a counter-moving test charge.  The file is closed afterwards, as the reference
+        closes it."""
         if Ezt is not None:
             self.Ezt = Ezt
             if self.Ez_hf is None:
@@ -215,8 +259,10 @@ class WakeSolver:
         keys = sorted(k for k in hf.keys() if isinstance(k, str) and k.startswith("#"))
         if not keys:
             raise IndexError("list index out of range")
-        s, it, zz, nz, nt = self._wp_index(len(keys))
-        ofs = [(1, 1)] if longitudinal else [(i, j) for i in (-1, 0, 1) for j in (-1, 0, 1)]
+        counter = bool(self.counter_moving) and not longitudinal
+        s, it, zz, nz, nt = self._wp_index(len(keys), counter)
+        nc = self.n_transverse_cells
+        ofs = [(1, 1)] if longitudinal else [(i, j) for i in range(-nc, nc + 1) for j in range(-nc, nc + 1)]
         ezt = np.zeros((len(ofs), nz, nt))
         ndim = np.ndim(hf[keys[0]])
         for n in range(nt):
@@ -228,19 +274,16 @@ class WakeSolver:
             else:
                 for li, (i, j) in enumerate(ofs):
                     ezt[li, :, n] = E[E.shape[0] // 2 + i, E.shape[1] // 2 + j, zz]
-        valid = it < nt
-        itw = np.where(it < 0, it + nt, it)
-        if np.any(valid & (itw < 0)):
-            bad = int(it[valid & (itw < 0)][0])
-            raise IndexError(f"index {bad} is out of bounds for axis 1 with size {nt}")
-        table = np.ascontiguousarray(np.where(valid, itw, -1).T, dtype=np.int32)  # (nz, ns)
-        dz = np.asarray(self.dz, dtype=np.float64)[:nz]
-        if len(ofs) == 9:
+        valid, itw = self._wrap(it, nt)
+        table = np.ascontiguousarray(np.where(valid, itw, -1).T, dtype=np.int32)  # (nz, ns), loop order
+        dz = self._loop_dz(nz, counter)
+        eloop = ezt[:, ::-1, :] if counter else ezt  # loop index k reads z index nz-1-k
+        if not longitudinal and nc >= 1:
             dxf, dyf = np.diff(self.xf), np.diff(self.yf)
-            wp3d, wpx, wpy = nat.wake_history(ezt, table, dz, self.q * 1e12, s[2] - s[1], dxf[0] + dxf[1],
-                                              dyf[0] + dyf[1])
+            wp3d, wpx, wpy = nat.wake_history(eloop, table, dz, self.q * 1e12, s[2] - s[1],
+                                              dxf[nc - 1] + dxf[nc], dyf[nc - 1] + dyf[nc])
         else:
-            wp3d, wpx, wpy = nat.wake_history(ezt, table, dz, self.q * 1e12)
+            wp3d, wpx, wpy = nat.wake_history(eloop, table, dz, self.q * 1e12)
         hf.close()
         self.Ez_hf = None
         return s, wp3d, wpx, wpy, ezt
@@ -262,12 +305,13 @@ class WakeSolver:
         for key, val in kwargs.items():
             setattr(self, key, val)
         if self._run is not None:
-            s, wp3d, wpx, wpy = self._finalize_device()
+            s, wp3d, wpx, wpy = self._finalize_device(transverse_lines=True)
         else:
             s, wp3d, wpx, wpy, _ = self._history_wp(False)
+        n = self.n_transverse_cells
         self.s = s
-        self.WP_3d = wp3d.reshape(3, 3, len(s))
-        self.WP = self.WP_3d[1, 1, :]
+        self.WP_3d = wp3d.reshape(2 * n + 1, 2 * n + 1, len(s))
+        self.WP = self.WP_3d[n, n, :]
         self._wpxy = (wpx, wpy)
         if self.save:
             self._savetxt("WP.txt", self.s, self.WP, "WP [V/pC]", "   s [m]")
@@ -279,6 +323,8 @@ class WakeSolver:
             setattr(self, key, val)
         if getattr(self, "_wpxy", None) is None:
             self.calc_long_WP_3d()
+        if self.n_transverse_cells < 1:  # the reference reads WP_3d[i0 + 1, ...] of a 1x1 WP_3d
+            raise IndexError("index 1 is out of bounds for axis 0 with size 1")
         self.WPx, self.WPy = self._wpxy
         if self.save:
             self._savetxt("WPx.txt", self.s, self.WPx, "WP [V/pC]", "   s [m]")
@@ -367,44 +413,63 @@ class WakeSolver:
     # ------------------------------------------------------------------ utilities
     @staticmethod
     def calc_impedance_from_wake(wake, s=None, t=None, fmax=None, samples=None, verbose=True):
-        """FFT of a wake function (wakis/wakeSolver.py:1185-1253)."""
-        if type(wake) is list:
-            t = wake[0]
-            wake = wake[1]
+        """Spectrum of a wake function, returned as [f, Z] with the conventions of the
+        reference's utility (wakis/wakeSolver.py:1185-1253).  The time axis is wake[0] when
+        wake is a list [t, W], else s/c, else t (AttributeError when none is given).  With
+        fmax the record is first resampled by linear interpolation onto a uniform axis of
+        step 1/(2 fmax) over [t.min(), t.max()); without it fmax = 1/dt.  The transform has
+        2*samples points (zero padding) or one point per sample, and the frequencies
+        0 <= f < fmax are kept, scaled by 2/len(record)."""
+        if isinstance(wake, list):
+            t, wake = wake[0], wake[1]
         if s is not None:
             t = s / c_light
-        elif s is None and t is None:
+        elif t is None:
             raise AttributeError('Provide time data through parameter "t" [s] or "s" [m]')
-        dt = np.mean(t[1:] - t[:-1])
-        if fmax is not None:
-            aux = np.arange(t.min(), t.max(), 1 / fmax / 2)
-            wake = np.interp(aux, t, wake)
-            dt = np.mean(aux[1:] - aux[:-1])
-        else:
-            fmax = 1 / dt
-        Wfft = np.fft.fft(wake, n=2 * samples) if samples is not None else np.fft.fft(wake)
-        ffft = np.fft.fftfreq(len(Wfft), dt)
-        mask = np.logical_and(ffft >= 0, ffft < fmax)
-        return [ffft[mask], Wfft[mask] / len(wake) * 2]
+        record, step = WakeSolver._uniform_record(np.asarray(t), np.asarray(wake),
+                                                  None if fmax is None else 1 / fmax / 2)
+        if fmax is None:
+            fmax = 1 / step
+        npts = record.shape[0]
+        nfft = npts if samples is None else 2 * samples
+        spectrum = np.fft.fft(record, n=nfft)
+        freqs = np.fft.fftfreq(nfft, step)
+        band = (freqs >= 0) & (freqs < fmax)
+        if verbose:
+            print(f"    * Number of samples = {int(band.sum())}")
+        return [freqs[band], spectrum[band] / npts * 2]
 
     @staticmethod
     def calc_wake_from_impedance(impedance, f=None, tmax=None, samples=None, pad=0, verbose=True):
-        """Inverse transform of an impedance (wakis/wakeSolver.py:1255-1315)."""
+        """Wake function of an impedance, returned as [t, W] with the conventions of the
+        reference's utility (wakis/wakeSolver.py:1255-1315): impedance is [f, Z] when it
+        has two entries, else Z with the frequencies in f (AttributeError without them).
+        With tmax, Z is resampled onto a uniform frequency axis of step 1/tmax; without it
+        tmax = 1/df.  W(t_i) = -Re(sum_b Z_b exp(-2 pi i b (i+1) / n)) over n = samples
+        points (len(Z) when samples is None), that is the transform advanced by one sample,
+        on t = n points evenly spaced over [0, tmax]."""
         if len(impedance) == 2:
             f, Z = impedance[0], impedance[1]
         elif f is None:
             raise AttributeError('Provide frequency data through parameter "f"')
         else:
             Z = impedance
-        df = np.mean(f[1:] - f[:-1])
-        if tmax is not None:
-            aux = np.arange(f.min(), f.max(), 1 / tmax)
-            Z = np.interp(aux, f, Z)
-        else:
-            tmax = 1 / df
-        wake = np.real(-1 * np.fft.fft(Z, n=samples))
-        wake = np.roll(wake, -1)
-        return [np.linspace(0, tmax, len(wake)), wake]
+        Z, step = WakeSolver._uniform_record(np.asarray(f), np.asarray(Z), None if tmax is None else 1 / tmax)
+        if tmax is None:
+            tmax = 1 / step
+        n = Z.shape[0] if samples is None else samples
+        spectrum = np.fft.fft(Z, n=n)
+        wake = -spectrum.real[(np.arange(n) + 1) % n]
+        return [np.linspace(0, tmax, n), wake]
+
+    @staticmethod
+    def _uniform_record(axis, values, spacing):
+        """(values, mean step) of a sampled record; with a spacing the record is first
+        interpolated linearly onto np.arange(axis.min(), axis.max(), spacing)."""
+        if spacing is None:
+            return values, np.mean(axis[1:] - axis[:-1])
+        uni = np.arange(axis.min(), axis.max(), spacing)
+        return np.interp(uni, axis, values), np.mean(uni[1:] - uni[:-1])
 
     def read_Ez(self, filename=None, return_value=False):
         """Opens an Ez line history (wakis/wakeSolver.py:1317-1364): an HDF5 file as the
@@ -466,28 +531,30 @@ class WakeSolver:
         else:
             self.log("[!] txt not saved, please provide x_data and y_data")
 
+    # the text files a run with save=True writes, in the order load_results reads them,
+    # with the attributes their two columns go to (None: the column is not kept)
+    _RESULT_FILES = (("lambda.txt", None, "lambdas"), ("WPx.txt", None, "WPx"), ("WPy.txt", None, "WPy"),
+                     ("WP.txt", "s", "WP"), ("spectrum.txt", None, "lambdaf"), ("Zx.txt", None, "Zx"),
+                     ("Zy.txt", None, "Zy"), ("Z.txt", "f", "Z"))
+
     def load_results(self, folder=None):
-        """Reads the results a run with save=True wrote (wakis/wakeSolver.py:1477-1511):
-        lambdas, WPx, WPy, s, WP, lambdaf, Zx, Zy, f (absolute value) and Z; sets
-        wakelength = s[-1], folder and Ez_file = folder + 'Ez.h5'."""
-        if folder is None and self.folder is None:
-            raise Exception("[!] Please provide a folder path")
-        elif folder is None:
+        """Reads back the results a run with save=True wrote (wakis/wakeSolver.py:1477-1511):
+        each file's two columns through read_txt; f is stored as its absolute value, the
+        wakelength is the last s, and folder and Ez_file (folder + 'Ez.h5') are set."""
+        if folder is None:
+            if self.folder is None:
+                raise Exception("[!] Please provide a folder path")
             folder = self.folder
-        if not folder.endswith("/"):
-            folder = folder + "/"
-        _, self.lambdas = self.read_txt(folder + "lambda.txt").values()
-        _, self.WPx = self.read_txt(folder + "WPx.txt").values()
-        _, self.WPy = self.read_txt(folder + "WPy.txt").values()
-        self.s, self.WP = self.read_txt(folder + "WP.txt").values()
-        _, self.lambdaf = self.read_txt(folder + "spectrum.txt").values()
-        _, self.Zx = self.read_txt(folder + "Zx.txt").values()
-        _, self.Zy = self.read_txt(folder + "Zy.txt").values()
-        self.f, self.Z = self.read_txt(folder + "Z.txt").values()
+        base = folder if folder.endswith("/") else folder + "/"
+        for fname, xattr, yattr in self._RESULT_FILES:
+            xcol, ycol = self.read_txt(base + fname).values()
+            if xattr is not None:
+                setattr(self, xattr, xcol)
+            setattr(self, yattr, ycol)
         self.f = np.abs(self.f)
         self.wakelength = self.s[-1]
-        self.folder = folder
-        self.Ez_file = folder + "Ez.h5"
+        self.folder = base
+        self.Ez_file = base + "Ez.h5"
 
     def _savetxt(self, name, a, b, label, xlabel):
         np.savetxt(self.folder + name, np.c_[a, b], header=xlabel + " " * 20 + label + "\n" + "-" * 48)
