@@ -301,7 +301,7 @@ def run_ours(args, rank, world):
             s._sync_coeffs()
             s._ensure_codes()
             s.fused_staging = args.staging
-            tuned = {tuple(args.fused_shape) + (args.staging,): float("nan")}
+            tuned = {tuple(args.fused_shape) + (args.staging, 1 if args.staging else 0): float("nan")}
         else:
             tuned = s.tune_fused()
     del mask
@@ -387,10 +387,13 @@ def run_ours(args, rank, world):
         shapes = {k: t for k, t in tuned.items() if k != "two-pass"}
         best = min(shapes, key=lambda t: shapes[t] if shapes[t] == shapes[t] else 0.0)
         out["fused_autotune"] = {"best": list(best),
-                                 "ms_per_step": {f"v{v}r{r}z{z}c{m}s{st}": t
-                                                 for (v, r, z, m, st), t in sorted(shapes.items())},
+                                 "ms_per_step": {f"v{v}r{r}z{z}c{m}s{st}a{a}": t
+                                                 for (v, r, z, m, st, a), t in sorted(shapes.items())},
                                  "two_pass_ms_per_step": tuned.get("two-pass")}
         out["config"]["kernels"] = "fused single-pass step (ping-pong field buffers)"
+        if len(best) > 4 and best[4]:
+            out["roofline"]["kernel"] = out["roofline"]["kernel"].replace("k_step_fused", "k_step_tma (TMA plane rings)")
+            out["config"]["kernels"] += ", old fields fed by TMA plane rings"
     else:
         out["config"]["kernels"] = f"{s.kernels} H and E pass kernels"
     csum = clk.summary(dev.index)

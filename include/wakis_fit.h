@@ -38,6 +38,7 @@ extern "C" {
 #define FIT_ERR_NOMEM (-5)
 #define FIT_ERR_DEVICE (-6)
 #define FIT_ERR_BUDGET (-7) /* a pool reservation would exceed the pool's memory budget */
+#define FIT_ERR_CANCELLED (-8) /* a pooled solve was cancelled (fit_pool_cancel) */
 
 #define FIT_F32 0
 #define FIT_F64 1
@@ -248,17 +249,28 @@ FIT_API int fit_set_coeff_codes(FitCtx *ctx, int32_t enable, int32_t *ncodes);
  * solver's autotuner times the candidates on the grid itself with fit_time_fused. */
 FIT_API int fit_set_fused_shape(FitCtx *ctx, int32_t vec, int32_t rows, int32_t zseg, int32_t ctas);
 /* How the fused step's old fields reach the threads (same results bit for bit):
- * staging 0 = per-thread global loads; 1 = tensor-memory-accelerator copies
- * (cp.async.bulk.tensor) of each plane's E, H and code boxes into shared-memory rings,
- * 4 E planes and 3 H / code planes deep; 2 = the same, 5 and 4 planes deep (with 4-row
- * tiles; 8-row tiles use the first depth).  The copies run on coded coefficients with Nx a multiple of 8 (and, in FP32,
- * the 4-wide vector); elsewhere the step keeps the loads.  The tile shape (rows 4: two
- * CTAs per SM, rows 8: one) and z ranges come from fit_set_fused_shape.  Needs the fused
+ * staging 0 = per-thread global loads; 1 or 2 = tensor-memory-accelerator copies
+ * (cp.async.bulk.tensor) of each plane's E, H and code boxes into shared-memory rings.
+ * With 4-row tiles, staging 1 sizes registers and shared memory for 3 CTAs per SM (rings
+ * of 4 E and 2 H / code planes), staging 2 for 4 CTAs per SM (3 and 2 planes); 8-row
+ * tiles run 2 CTAs per SM (3 and 2 planes) for either.  The copies run on coded
+ * coefficients with Nx a multiple of 8 (and, in FP32, the 4-wide vector); elsewhere the
+ * step keeps the loads.  l2_ahead (0..16): with the copies, the same boxes of that many
+ * further planes are requested into L2 (cp.async.bulk.prefetch.tensor) ahead of the ring
+ * loads, so those hit L2; 0 turns it off.  The rows and z ranges come from
+ * fit_set_fused_shape.  Needs the fused
  * step enabled (FIT_ERR_STATE otherwise); returns FIT_ERR_ARG when the grid does not
  * qualify or the tensor maps cannot be encoded.
  * Same work as fit_set_fused_shape's kernel: the reference's _one_step
  * (wakis/solverFIT3D.py:504-525). */
-FIT_API int fit_set_fused_staging(FitCtx *ctx, int32_t staging);
+FIT_API int fit_set_fused_staging(FitCtx *ctx, int32_t staging, int32_t l2_ahead);
+/* Polls a kernel makes on a bounded wait for its bulk or tensor copies before it gives
+ * up, records FIT_ERR_TIMEOUT (read by fit_check_error) and returns with its fields
+ * unchanged from that point (staged passes, TMA-fed fused step).  Default 2^24; 0 gives up
+ * at the first wait, which exercises the failure path without a fault.  After giving up a
+ * kernel still waits (2^24 polls at most) for the copies it issued.  No counterpart in the
+ * reference (its scipy step has no waits). */
+FIT_API int fit_set_wait_limit(FitCtx *ctx, int64_t polls);
 /* Times, beam off, on the context stream between CUDA events: reps fused steps from
  * (E, H) into the second buffers (ms_out[0]), and reps two-pass steps (H pass + E pass)
  * in place on copies of E and H in the second buffers (ms_out[1]); average milliseconds
@@ -290,7 +302,7 @@ typedef struct FitPool FitPool;
 typedef struct FitPoolDone {
     int64_t tag;       /* the tag given to fit_pool_submit */
     int64_t steps;     /* steps taken */
-    int32_t status;    /* FIT_OK, or the error that stopped the pool */
+    int32_t status;    /* FIT_OK, FIT_ERR_CANCELLED, or the error that stopped the pool */
     int32_t reserved;
     double t_submit_ms; /* host times in ms since fit_pool_create: submitted, */
     double t_start_ms;  /* first chunk containing the context launched, */
@@ -333,6 +345,14 @@ FIT_API int fit_pool_submit(FitPool *pool, FitCtx *ctx, int64_t n0, int64_t nste
 /* Copies up to max finished solves into out and returns how many (>= 0), waiting up to
  * wait_ms for the first one when none is ready and work is pending. */
 FIT_API int fit_pool_poll(FitPool *pool, FitPoolDone *out, int32_t max, int32_t wait_ms);
+/* Cancels the solve submitted with tag: a queued one is reported at once, a running one
+ * gets no further chunks and is reported once the chunks in flight that step it have
+ * completed, with status FIT_ERR_CANCELLED (unless those chunks took its last steps:
+ * then it is reported finished, FIT_OK).  The other solves are not affected.  The
+ * context is then usable again (its fields hold the steps taken).  FIT_ERR_ARG when no
+ * queued or running solve has that tag.  No counterpart in the reference (one solve per
+ * process). */
+FIT_API int fit_pool_cancel(FitPool *pool, int64_t tag);
 FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
 /* Chooses the pass kernels of one vector-width class (vec = 4, 2 or 1 cells per vector,
  * the widest that divides Nx): ctas_per_sm names the compiled variant by the CTAs per SM
@@ -364,6 +384,15 @@ FIT_API int fit_set_monitor(FitCtx *ctx, int32_t nf, const double *phases, int64
  * nsteps*nlines*Nz values).  nlines = 0 stops recording. */
 FIT_API int fit_set_ez_record(FitCtx *ctx, void *hist, int32_t nlines, const int32_t *lx, const int32_t *ly,
                               int64_t n0, int64_t nsteps);
+/* J_z line history of wakesolve(save_J=True) (wakis/routines.py:440-445), taken by the
+ * step prologue like the Ez record: for steps n0 <= n < n0+nsteps, hist (device,
+ * nsteps*nlines*Nz values of the field dtype) receives per line J_z after the beam
+ * update and before the step -- the beam current on the beam's line, elsewhere
+ * sigma_z*E_z of the previous step (a float64 product stored in the field dtype, as the
+ * reference's J = sigma*E).  sigma_lines: host, nlines*Nz FP64 values of sigma_z on the
+ * lines.  nlines = 0 turns the record off. */
+FIT_API int fit_set_jz_record(FitCtx *ctx, void *hist, int32_t nlines, const int32_t *lx, const int32_t *ly,
+                              int64_t n0, int64_t nsteps, const double *sigma_lines);
 
 /* Library build information: sm architecture compiled for, and the kernel launch
  * counter (kernels issued since load), for bench accounting. */

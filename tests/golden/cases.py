@@ -280,6 +280,32 @@ def resonator_H(N, dt):
     return Hx, Hy, Hz, (xmin, xmin + L)
 
 
+# ----------------------------------------------------------------------------- checkpoints
+# save_state after save_at steps of a user loop, a fresh solver load_state + the remaining
+# steps, and the uninterrupted run (wakis/solverFIT3D.py:908-1035); emsolve(save=True)
+# (wakis/routines.py:122-204) on a small PEC box.
+CHECKPOINT_CASES = {
+    "checkpoint_pmc_beam_f64": dict(base="pmc_beam_f64", save_at=17),
+}
+EMSOLVE_SAVE_CASE = dict(grid=dict(xmin=-1.0, xmax=1.0, ymin=-1.0, ymax=1.0, zmin=-1.0, zmax=1.0, Nx=8, Ny=8, Nz=8),
+                         Nt=4, fields=["E", "Hy"], components=["Abs", "z"])
+
+
+# ----------------------------------------------------------------------------- mesh refinement
+# GridFIT3D.refine_axis (wakis/gridFIT3D.py:771-859) on seeded snap sets: (seed, xmin, xmax,
+# nodes, number of snaps, method)
+REFINE_CASES = [(31, -0.06, 0.06, 31, 4, "insert"), (32, -0.06, 0.06, 31, 4, "neighbor"),
+                (33, 0.0, 1.0, 25, 6, "insert"), (34, -1.0, 2.0, 41, 3, "neighbor"),
+                (35, -0.2, 0.2, 17, 2, "insert"), (36, 0.0, 0.5, 60, 9, "neighbor")]
+
+
+def refine_snaps(seed, xmin, xmax, nsnap):
+    """Snap coordinates of a refinement case: the domain bounds and nsnap interior points."""
+    rng = np.random.default_rng(seed)
+    inner = np.sort(rng.uniform(xmin + 0.05 * (xmax - xmin), xmax - 0.05 * (xmax - xmin), nsnap))
+    return np.unique(np.concatenate(([xmin], np.round(inner, 5), [xmax])))
+
+
 # ----------------------------------------------------------------------------- full configs
 # The benchmark workloads at full size (geometry analytic, evaluated at cell centres).
 CONFIGS = {

@@ -145,6 +145,76 @@ def run_userloop(wakis, name, case, out):
     out[name] = dict(dt=np.float64(solver.dt), E=solver.E.toarray(), H=solver.H.toarray(), J=solver.J.toarray())
 
 
+def run_checkpoint(wakis, name, spec, out):
+    """save_state after save_at steps of a user loop, the saved datasets as read back
+    through read_state, a fresh solver's load_state + the remaining steps, and the first
+    solver continued without interruption."""
+    case = C.CASES[spec["base"]]
+    n1, nt = spec["save_at"], case["Nt"]
+    solver = make_solver(wakis, case, make_grid(wakis, case))
+    beam = wakis.sources.Beam(**case["beam"])
+    for n in range(n1):
+        beam.update(solver, n * solver.dt)
+        solver.one_step()
+    solver.save_state("state.h5")
+    st = solver.read_state("state.h5")
+    keys = sorted(st.keys())
+    saved = {k: np.array(st[k]) for k in keys}
+    st.close()
+    s2 = make_solver(wakis, case, make_grid(wakis, case))
+    s2.load_state("state.h5")
+    beam2 = wakis.sources.Beam(**case["beam"])
+    for n in range(n1, nt):
+        beam2.update(s2, n * s2.dt)
+        s2.one_step()
+    for n in range(n1, nt):
+        beam.update(solver, n * solver.dt)
+        solver.one_step()
+    res = dict(keys=np.array(keys), dt=np.float64(solver.dt))
+    for k, v in saved.items():
+        res["saved_" + k] = v
+    for k in ("E", "H", "J"):
+        res["restart_" + k] = np.array(getattr(s2, k).toarray())  # copies: reset_fields zeroes in place
+        res["cont_" + k] = np.array(getattr(solver, k).toarray())
+    s2.reset_fields()
+    res["reset_max"] = np.float64(max(np.abs(getattr(s2, k).toarray()).max() for k in ("E", "H", "J")))
+    out[name] = res
+
+
+def run_refine(wakis, out):
+    """GridFIT3D.refine_axis of the reference on the seeded snap sets of REFINE_CASES, and
+    the exception its 'subdivision' method raises."""
+    g = wakis.GridFIT3D(0, 1, 0, 1, 0, 1, 2, 2, 2, verbose=0)
+    res = {}
+    for i, (seed, lo, hi, n, ns, method) in enumerate(C.REFINE_CASES):
+        res[f"x{i}"] = g.refine_axis(lo, hi, n, C.refine_snaps(seed, lo, hi, ns), method=method)
+    try:
+        g.refine_axis(0.0, 1.0, 11, np.array([0.0, 0.37, 1.0]), method="subdivision")
+        err = ("", "")
+    except Exception as e:  # the reference's own failure is the fixture
+        err = (type(e).__name__, str(e))
+    res["subdivision_exc"] = np.array(err)
+    out["refine_axis"] = res
+
+
+def run_emsolve_save(wakis, out):
+    """emsolve(save=True): the exception the reference raises and the files it leaves."""
+    spec = C.EMSOLVE_SAVE_CASE
+    g = spec["grid"]
+    grid = wakis.GridFIT3D(g["xmin"], g["xmax"], g["ymin"], g["ymax"], g["zmin"], g["zmax"], g["Nx"], g["Ny"],
+                           g["Nz"], verbose=0)
+    solver = wakis.SolverFIT3D(grid, bc_low=["pec"] * 3, bc_high=["pec"] * 3, verbose=0)
+    before = set(os.listdir("."))
+    err = ("", "")
+    try:
+        solver.emsolve(spec["Nt"], save=True, fields=spec["fields"], components=spec["components"])
+    except Exception as e:  # the reference's own failure is the fixture
+        err = (type(e).__name__, str(e))
+    files = sorted(set(os.listdir(".")) - before)
+    out["emsolve_save"] = dict(exc_type=np.array(err[0]), exc_msg=np.array(err[1]), files=np.array(files),
+                               nstep=np.int64(getattr(solver, "nstep", 0)))
+
+
 def run_wakefile(wakis, name, case, out):
     """The reference's WakeSolver post-processing of a synthetic Ez file (written through
     the h5py stand-in), without a solver run."""
@@ -226,6 +296,17 @@ def main():
                     continue
                 print("case", name, flush=True)
                 run_wakefile(wakis, name, case, out)
+            for name, spec in C.CHECKPOINT_CASES.items():
+                if a.only and name != a.only:
+                    continue
+                print("case", name, flush=True)
+                run_checkpoint(wakis, name, spec, out)
+            if not a.only or a.only == "refine_axis":
+                print("case refine_axis", flush=True)
+                run_refine(wakis, out)
+            if not a.only or a.only == "emsolve_save":
+                print("case emsolve_save", flush=True)
+                run_emsolve_save(wakis, out)
             if a.test001:
                 inp = test001_inputs(ref_root)
                 res = run_test001(wakis, inp)

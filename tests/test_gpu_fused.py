@@ -196,11 +196,11 @@ def test_tma_staging_rejected_where_it_does_not_apply():
     s._sync_coeffs()
     s._ensure_codes()
     with pytest.raises(nat.FitError):
-        s._ctx.call("fit_set_fused_staging", 1)
+        s._ctx.call("fit_set_fused_staging", 1, 1)
     s2 = _random_field_solver(np.linspace(-1, 1, 17), np.linspace(-0.8, 0.7, 14), np.linspace(-2, 2, 41),
                               np.float32, False)
     s2._sync_coeffs()
     s2._ensure_codes()
     with pytest.raises(nat.FitError):
-        s2._ctx.call("fit_set_fused_staging", 1)
+        s2._ctx.call("fit_set_fused_staging", 1, 1)
     assert isinstance(s2, wg.SolverFIT3D)

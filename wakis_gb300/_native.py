@@ -16,9 +16,11 @@ FIT_F32, FIT_F64 = 0, 1
 FIT_BC = {"periodic": 0, "pec": 1, "electric": 1, "pml": 2, "pmc": 3, "magnetic": 3, "abc": 4}
 FIT_J_ELIDED, FIT_J_EXPLICIT = 0, 1
 
+FIT_ERR_TIMEOUT = -4
 FIT_ERR_BUDGET = -7
+FIT_ERR_CANCELLED = -8
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "invalid state", -4: "timeout", -5: "out of memory",
-           -6: "no device", -7: "over the pool budget"}
+           -6: "no device", -7: "over the pool budget", -8: "cancelled"}
 
 
 class FitError(RuntimeError):
@@ -87,11 +89,13 @@ _SIGS = {
     "fit_set_kernel_variant": (_P, C.c_int32),
     "fit_time_fused": (_P, C.c_int32, _D),
     "fit_set_fused_shape": (_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32),
-    "fit_set_fused_staging": (_P, C.c_int32),
+    "fit_set_fused_staging": (_P, C.c_int32, C.c_int32),
+    "fit_set_wait_limit": (_P, C.c_int64),
     "fit_set_coeff_codes": (_P, C.c_int32, C.POINTER(C.c_int32)),
     "fit_monitor_update": (_P, C.c_int32, C.c_int64, C.c_int32, _D, _P, C.c_int32, _P),
     "fit_set_monitor": (_P, C.c_int32, _D, C.c_int64, C.c_int64, _P, C.c_int32),
     "fit_set_ez_record": (_P, _P, C.c_int32, _I32, _I32, C.c_int64, C.c_int64),
+    "fit_set_jz_record": (_P, _P, C.c_int32, _I32, _I32, C.c_int64, C.c_int64, _D),
     "fit_pool_create": (C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)),
     "fit_pool_destroy": (_P,),
     "fit_pool_last_error": (_P, C.c_char_p, C.c_int64),
@@ -99,6 +103,7 @@ _SIGS = {
     "fit_pool_release": (_P, C.c_int64),
     "fit_pool_submit": (_P, _P, C.c_int64, C.c_int64, C.c_int64),
     "fit_pool_poll": (_P, C.POINTER(FitPoolDone), C.c_int32, C.c_int32),
+    "fit_pool_cancel": (_P, C.c_int64),
     "fit_pool_stats": (_P, C.POINTER(FitPoolStats)),
     "fit_pool_tune": (_P, C.c_int32, C.c_int32),
     "fit_version": (C.c_char_p, C.c_int64),
@@ -277,6 +282,12 @@ class Pool:
         n = self._check(self.lib.fit_pool_poll(self.h, out, max_n, int(wait_ms)))
         return [dict(tag=d.tag, steps=d.steps, status=d.status, t_submit_ms=d.t_submit_ms,
                      t_start_ms=d.t_start_ms, t_done_ms=d.t_done_ms) for d in out[:n]]
+
+    def cancel(self, tag):
+        """Cancels a queued or running solve: poll() reports it with status
+        FIT_ERR_CANCELLED once no chunk in flight steps it (or FIT_OK if its last steps
+        were already in flight)."""
+        self._check(self.lib.fit_pool_cancel(self.h, int(tag)))
 
     def stats(self):
         s = FitPoolStats()

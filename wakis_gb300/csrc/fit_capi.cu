@@ -91,11 +91,15 @@ struct FitCtx {
     void *E2 = nullptr, *H2 = nullptr;  // the second field buffers of the fused step
     int fused_vec = 4, fused_rows = 8, fused_zseg = 1, fused_ctas = 2;  // tile shape of the fused step
     int fused_staging = 0;  // 0: loads; 1, 2: TMA plane rings (fit_set_fused_staging)
+    long long wait_limit = kWaitLimit;  // polls of the bounded waits for data (fit_set_wait_limit)
+    int tma_prefetch = 1;  // planes the TMA-fed step's L2 prefetch runs ahead of its ring loads
     bool graph_fused = false;  // the cached graph holds fused steps
     unsigned short* d_code = nullptr;  // coded coefficients: one code per cell (nullptr: dense)
     void* d_tab = nullptr;             // [code][ch, ce, cl][x, y, z, pad] in the field dtype
     int ncodes = 0;
     RecordArgs rec{};           // Ez line history of recorded steps (nlines = 0: off)
+    JRecordArgs jrec{};         // Jz line history of recorded steps (nlines = 0: off)
+    double* d_jsig = nullptr;   // sigma_z on the Jz record lines
     MonitorArgs mon{};          // field monitor epilogue of device-loop steps (nf = 0: off)
     double2* d_mon_phases = nullptr;
     std::atomic<bool> in_pool{false};  // submitted to a FitPool and not yet reported done
@@ -186,6 +190,18 @@ int leave(FitCtx* c) {
     CK(cudaEventRecord(c->ev_out, c->own));
     CK(cudaStreamWaitEvent(c->user, c->ev_out, 0));
     return FIT_OK;
+}
+
+// the Jz record arguments of a launch: the beam as it is for this step
+JRecordArgs jrec_args(const FitCtx* c) {
+    JRecordArgs j = c->jrec;
+    if (j.nlines > 0) {
+        j.beam = c->beam;
+        j.vt_table = c->d_vt_table;
+        j.vt_len = c->vt_len;
+        j.vt_host = c->beam_vt;
+    }
+    return j;
 }
 
 int pick_vec(const FitCtx* c) {
@@ -281,7 +297,7 @@ void launch_h(FitCtx* c) {
         auto k = k_hpass_staged<T, VEC, kNstH, kTpbH>;
         allow_smem(k, sm);
         k<<<c->nsm, kTpbH, sm, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
-                                       static_cast<const T*>(c->ch), c->g, metric<T>(c), c->d_err);
+                                       static_cast<const T*>(c->ch), c->g, metric<T>(c), c->d_err, c->wait_limit);
     } else if (c->d_code) {
         const long long nv = c->g.N / VEC;
         k_hpass_coded<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E),
@@ -311,13 +327,13 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
             auto k = k_epass_staged<T, VEC, kNstE, 1, kTpbE>;
             allow_smem(k, sm);
             k<<<c->nsm, kTpbE, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
-                                           c->d_err);
+                                           c->d_err, c->wait_limit);
         } else {
             const size_t sm = staged_bytes<T, VEC, 13, kNstE, kTpbE>();
             auto k = k_epass_staged<T, VEC, kNstE, 0, kTpbE>;
             allow_smem(k, sm);
             k<<<c->nsm, kTpbE, sm, c->own>>>(E, H, ce, cl, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
-                                           c->d_err);
+                                           c->d_err, c->wait_limit);
         }
         count(c);
         return;
@@ -363,10 +379,11 @@ void launch_step_t(FitCtx* c, long long n, int mode, bool device_step) {
         st.n = n;
         st.vt = c->beam_vt;
     }
-    const bool need_pro = device_step || c->plane.active || c->tap.nlines > 0 || c->rec.nlines > 0;
+    const bool need_pro =
+        device_step || c->plane.active || c->tap.nlines > 0 || c->rec.nlines > 0 || c->jrec.nlines > 0;
     if (need_pro) {
         k_prologue<T><<<1, 512, 0, c->own>>>(static_cast<T*>(c->E), static_cast<T*>(c->H), c->g, c->plane, c->tap,
-                                             n, device_step ? c->d_step : nullptr, c->rec);
+                                             n, device_step ? c->d_step : nullptr, c->rec, jrec_args(c));
         count(c);
     }
     const int vec = pick_vec(c);
@@ -533,39 +550,44 @@ bool launch_tma_shape(FitCtx* c, int mode, const StepArgs& st, bool forward, con
         auto k = k_step_tma<T, VEC, FY, MB, 1, NE, NH>;
         allow_smem(k, L::BYTES);
         k<<<grid, block, L::BYTES, c->own>>>(mE, mH, mC, Ein, Hin, Eout, Hout, J, c->use_cond, c->g, metric<T>(c),
-                                             beam, st, zlen, c->d_code, tab, c->d_err);
+                                             beam, st, zlen, c->d_code, tab, c->d_err, c->wait_limit,
+                                             c->tma_prefetch);
     } else {
         auto k = k_step_tma<T, VEC, FY, MB, 0, NE, NH>;
         allow_smem(k, L::BYTES);
         k<<<grid, block, L::BYTES, c->own>>>(mE, mH, mC, Ein, Hin, Eout, Hout, J, c->use_cond, c->g, metric<T>(c),
-                                             beam, st, zlen, c->d_code, tab, c->d_err);
+                                             beam, st, zlen, c->d_code, tab, c->d_err, c->wait_limit,
+                                             c->tma_prefetch);
     }
     count(c);
     return true;
 }
 
-// 4 rows: two CTAs per SM; 8 rows: one
+// tile shapes (rows, CTAs per SM, E ring depth, H ring depth): 4 rows and 3 CTAs per SM
+// with rings of 4 / 2 planes (staging 1); 4 rows and 4 CTAs per SM with 3 / 2 (staging
+// 2, shared memory and registers sized for four); 8 rows, 2 CTAs per SM, 3 / 2
 template <typename T, int VEC>
 bool launch_tma(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
-    if (c->fused_rows == 8) return launch_tma_shape<T, VEC, 8, 1, 4, 3>(c, mode, st, forward, beam);
-    if (c->fused_staging == 2) return launch_tma_shape<T, VEC, 4, 2, 5, 4>(c, mode, st, forward, beam);
-    return launch_tma_shape<T, VEC, 4, 2, 4, 3>(c, mode, st, forward, beam);
+    if (c->fused_rows == 8) return launch_tma_shape<T, VEC, 8, 2, 3, 2>(c, mode, st, forward, beam);
+    if (c->fused_staging == 2) return launch_tma_shape<T, VEC, 4, 4, 3, 2>(c, mode, st, forward, beam);
+    return launch_tma_shape<T, VEC, 4, 3, 4, 2>(c, mode, st, forward, beam);
+}
+
+template <typename T, int VEC>
+bool tma_maps_ok_t(const FitCtx* c, int staging, int rows, bool forward) {
+    CUtensorMap a, b, d;
+    if (rows == 8) return encode_step_maps<T, VEC, 8, 3, 2>(c, forward, &a, &b, &d);
+    if (staging == 2) return encode_step_maps<T, VEC, 4, 3, 2>(c, forward, &a, &b, &d);
+    return encode_step_maps<T, VEC, 4, 4, 2>(c, forward, &a, &b, &d);
 }
 
 bool tma_maps_ok(const FitCtx* c, int staging, int rows) {
-    CUtensorMap a, b, d;
-    bool ok = true;
-    for (int f = 0; f < 2 && ok; ++f) {
-        if (c->dtype == FIT_F64)
-            ok = rows == 8 ? encode_step_maps<double, 2, 8, 4, 3>(c, f == 0, &a, &b, &d)
-                 : staging == 2 ? encode_step_maps<double, 2, 4, 5, 4>(c, f == 0, &a, &b, &d)
-                                : encode_step_maps<double, 2, 4, 4, 3>(c, f == 0, &a, &b, &d);
-        else
-            ok = rows == 8 ? encode_step_maps<float, 4, 8, 4, 3>(c, f == 0, &a, &b, &d)
-                 : staging == 2 ? encode_step_maps<float, 4, 4, 5, 4>(c, f == 0, &a, &b, &d)
-                                : encode_step_maps<float, 4, 4, 4, 3>(c, f == 0, &a, &b, &d);
+    for (int f = 0; f < 2; ++f) {
+        const bool ok = c->dtype == FIT_F64 ? tma_maps_ok_t<double, 2>(c, staging, rows, f == 0)
+                                            : tma_maps_ok_t<float, 4>(c, staging, rows, f == 0);
+        if (!ok) return false;
     }
-    return ok;
+    return true;
 }
 
 void launch_fused(FitCtx* c, int mode, const StepArgs& st, bool forward, const BeamArgs& beam) {
@@ -600,14 +622,14 @@ void launch_fused_step(FitCtx* c, int mode, bool forward, const StepArgs& st, lo
     if (c->dtype == FIT_F64) {
         k_prologue<double><<<1, 512, 0, c->own>>>(static_cast<double*>(forward ? c->E : c->E2),
                                                    static_cast<double*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
-                                                   n, dev ? c->d_step : nullptr, c->rec);
+                                                   n, dev ? c->d_step : nullptr, c->rec, jrec_args(c));
         count(c);
         launch_fused(c, mode, st, forward, c->beam);
         launch_monitor<double>(c, static_cast<const double*>(forward ? c->E2 : c->E), dev, n);
     } else {
         k_prologue<float><<<1, 512, 0, c->own>>>(static_cast<float*>(forward ? c->E : c->E2),
                                                  static_cast<float*>(forward ? c->H : c->H2), c->g, c->plane, c->tap,
-                                                 n, dev ? c->d_step : nullptr, c->rec);
+                                                 n, dev ? c->d_step : nullptr, c->rec, jrec_args(c));
         count(c);
         launch_fused(c, mode, st, forward, c->beam);
         launch_monitor<float>(c, static_cast<const float*>(forward ? c->E2 : c->E), dev, n);
@@ -806,7 +828,7 @@ int fit_ctx_destroy(FitCtx* c) {
         dfree(c->L_T[a], c->own);
     }
     for (void* p : {c->ch, c->ce, c->cl, c->cj, c->sg, c->E2, c->H2, (void*)c->d_mon_phases, (void*)c->d_code,
-                    c->d_tab})
+                    c->d_tab, (void*)c->d_jsig})
         dfree(p, c->own);
     for (void* p : {(void*)c->d_beam_z, (void*)c->d_beam_dtieps, (void*)c->d_vt_table, (void*)c->d_prof,
                     (void*)c->d_c1, (void*)c->d_c2, (void*)c->d_gt, (void*)c->d_stash, (void*)c->d_base, (void*)c->d_row,
@@ -1477,6 +1499,15 @@ int fit_check_error(FitCtx* c) {
     return FIT_OK;
 }
 
+int fit_set_wait_limit(FitCtx* c, int64_t polls) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    if (polls < 0) return fail(c, FIT_ERR_ARG, "polls must be >= 0 (0: give up at once)");
+    invalidate(c);
+    c->wait_limit = polls;
+    return FIT_OK;
+}
+
 int fit_set_kernel_variant(FitCtx* c, int32_t variant) {
     if (!c) return FIT_ERR_ARG;
     if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
@@ -1537,10 +1568,11 @@ int fit_set_fused_shape(FitCtx* c, int32_t vec, int32_t rows, int32_t zseg, int3
     return FIT_OK;
 }
 
-int fit_set_fused_staging(FitCtx* c, int32_t staging) {
+int fit_set_fused_staging(FitCtx* c, int32_t staging, int32_t l2_ahead) {
     if (!c) return FIT_ERR_ARG;
     if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
     if (staging < 0 || staging > 2) return fail(c, FIT_ERR_ARG, "staging must be 0 (loads), 1 or 2 (TMA rings)");
+    if (l2_ahead < 0 || l2_ahead > 16) return fail(c, FIT_ERR_ARG, "l2_ahead must be in [0, 16]");
     if (staging != 0) {
         if (!c->fused || !c->E2) return fail(c, FIT_ERR_STATE, "the fused step is not enabled for this context");
         if (!tma_grid_ok(c))
@@ -1550,6 +1582,7 @@ int fit_set_fused_staging(FitCtx* c, int32_t staging) {
     }
     invalidate(c);
     c->fused_staging = staging;
+    c->tma_prefetch = l2_ahead;
     return FIT_OK;
 }
 
@@ -1599,6 +1632,37 @@ int fit_set_ez_record(FitCtx* c, void* hist, int32_t nlines, const int32_t* lx, 
     r.nsteps = nsteps;
     c->rec = r;
     return FIT_OK;
+}
+
+int fit_set_jz_record(FitCtx* c, void* hist, int32_t nlines, const int32_t* lx, const int32_t* ly, int64_t n0,
+                      int64_t nsteps, const double* sigma_lines) {
+    if (!c) return FIT_ERR_ARG;
+    if (c->in_pool) return fail(c, FIT_ERR_STATE, "the context is running in a pool");
+    invalidate(c);
+    if (nlines <= 0) {
+        c->jrec = JRecordArgs{};
+        return FIT_OK;
+    }
+    if (nlines > 9 || !hist || !lx || !ly || !sigma_lines || n0 < 0 || nsteps <= 0)
+        return fail(c, FIT_ERR_ARG, "bad Jz record arguments");
+    JRecordArgs r{};
+    for (int l = 0; l < nlines; ++l) {
+        if (lx[l] < 0 || lx[l] >= c->g.nx || ly[l] < 0 || ly[l] >= c->g.ny)
+            return fail(c, FIT_ERR_ARG, "Jz record line %d outside the grid", l);
+        r.base[l] = (long long)lx[l] + c->g.sy * ly[l];
+    }
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = upload(c, &c->d_jsig, sigma_lines, (size_t)nlines * c->g.nz * sizeof(double));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->own));
+    r.hist = hist;
+    r.nlines = nlines;
+    r.n0 = n0;
+    r.nsteps = nsteps;
+    r.sig = c->d_jsig;
+    c->jrec = r;
+    return leave(c);
 }
 
 int fit_time_fused(FitCtx* c, int32_t reps, double* ms_out) {

@@ -1021,8 +1021,8 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
 // computes from shared memory while the next NST-1 chunks are in flight.  DRAM
 // latency is covered by the copies in flight, not by warp occupancy.  Requirements:
 // Nx*sizeof(T) is a multiple of 16 bytes (all stream starts are then 16-byte aligned).
-// Every wait is bounded: on expiry the kernel records FIT_ERR_TIMEOUT in *err, waits
-// (bounded) for its own copies and returns.
+// Every wait is bounded (wlim polls): on expiry the kernel records FIT_ERR_TIMEOUT in
+// *err, waits (bounded by kWaitLimit) for its own copies and returns.
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -1062,7 +1062,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     return false;
 }
 
-constexpr long long kWaitLimit = 1LL << 24;  // try_wait polls (each waits up to ~a microsecond)
+// try_wait polls of a bounded wait (each waits up to ~a microsecond).  The waits for data
+// take the context's limit (kWaitLimit unless fit_set_wait_limit changed it: a test of the
+// give-up path sets 0); the drains after giving up always use kWaitLimit, so no copy lands
+// in the shared memory of a CTA that has exited.
+constexpr long long kWaitLimit = 1LL << 24;
 
 struct Stream {
     int src;         // which input array (kernel specific)
@@ -1106,7 +1110,8 @@ __device__ __forceinline__ void lds_v(T (&r)[VEC], const T* p) {
 // 7-9 H, 10-12 ch
 template <typename T, int VEC, int NST, int TPB>
 __global__ void __launch_bounds__(TPB, 1) k_hpass_staged(const T* __restrict__ E, T* __restrict__ H,
-                                                         const T* __restrict__ ch, Geom g, Metric<T> mt, int* err) {
+                                                         const T* __restrict__ ch, Geom g, Metric<T> mt, int* err,
+                                                         long long wlim) {
     constexpr int A = 16 / sizeof(T);
     constexpr int CH = TPB * VEC;
     constexpr int NS = 13;
@@ -1143,7 +1148,7 @@ __global__ void __launch_bounds__(TPB, 1) k_hpass_staged(const T* __restrict__ E
         const int s = (int)(it % NST);
         const unsigned parity = (unsigned)((it / NST) & 1);
         // every thread waits; the decision to give up is CTA-uniform
-        if (!__syncthreads_and(mbar_wait(&bars[s], parity, kWaitLimit))) {
+        if (!__syncthreads_and(mbar_wait(&bars[s], parity, wlim))) {
             ok = false;
             break;
         }
@@ -1200,7 +1205,8 @@ template <typename T, int VEC, int NST, int MODE, int TPB>
 __global__ void __launch_bounds__(TPB, 1) k_epass_staged(T* __restrict__ E, const T* __restrict__ H,
                                                          const T* __restrict__ ce, const T* __restrict__ cl,
                                                          T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
-                                                         BeamArgs b, PlaneArgs pl, StepArgs stp, int* err) {
+                                                         BeamArgs b, PlaneArgs pl, StepArgs stp, int* err,
+                                                         long long wlim) {
     constexpr int A = 16 / sizeof(T);
     constexpr int CH = TPB * VEC;
     constexpr int NS = MODE == 1 ? 16 : 13;
@@ -1246,7 +1252,7 @@ __global__ void __launch_bounds__(TPB, 1) k_epass_staged(T* __restrict__ E, cons
         const int s = (int)(it % NST);
         const unsigned parity = (unsigned)((it / NST) & 1);
         // every thread waits; the decision to give up is CTA-uniform
-        if (!__syncthreads_and(mbar_wait(&bars[s], parity, kWaitLimit))) {
+        if (!__syncthreads_and(mbar_wait(&bars[s], parity, wlim))) {
             ok = false;
             break;
         }
@@ -1631,9 +1637,26 @@ struct RecordArgs {
     long long n0, nsteps;
 };
 
+// J_z line history (the reference's Jz.h5 dump of wakesolve(save_J=True),
+// wakis/routines.py:440-445): J_z on the recorded lines after the beam update and before
+// the step.  J is sigma*E of the previous step there (the reference's J = sigma*E, a
+// float64 product stored in the field dtype), and the beam current on the beam line.
+struct JRecordArgs {
+    void* hist;  // [step][line][k] in the field dtype
+    int nlines;
+    int pad;
+    long long base[9];  // flat index of J_z(lx, ly, 0) per line
+    long long n0, nsteps;
+    const double* sig;  // sigma_z on the lines, [line][k] (device)
+    BeamArgs beam;
+    const double* vt_table;  // device loops: v*t of step n
+    long long vt_len;
+    double vt_host;  // host-driven steps: v*t of this step
+};
+
 template <typename T>
 __global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneArgs pl, TapArgs tp,
-                           long long n_arg, long long* d_step, RecordArgs rec) {
+                           long long n_arg, long long* d_step, RecordArgs rec, JRecordArgs jr) {
     const long long n = d_step ? *d_step : n_arg;
     // plane source
     if (pl.active && n >= 0 && n < pl.len) {
@@ -1654,6 +1677,18 @@ __global__ void k_prologue(T* __restrict__ E, T* __restrict__ H, Geom g, PlaneAr
         for (int t = threadIdx.x; t < rec.nlines * g.nz; t += blockDim.x) {
             const int l = t / g.nz, k = t - l * g.nz;
             h[t] = Ez[rec.base[l] + g.sz * k];
+        }
+    }
+    if (jr.nlines > 0 && n >= jr.n0 && n < jr.n0 + jr.nsteps) {
+        T* h = static_cast<T*>(jr.hist) + (n - jr.n0) * jr.nlines * (long long)g.nz;
+        const T* Ez = E + 2 * g.N;
+        const double vt = d_step ? ((jr.vt_table && n < jr.vt_len) ? jr.vt_table[n] : 0.0) : jr.vt_host;
+        for (int t = threadIdx.x; t < jr.nlines * g.nz; t += blockDim.x) {
+            const int l = t / g.nz, k = t - l * g.nz;
+            if (jr.beam.active && jr.base[l] == jr.beam.ixs + g.sy * jr.beam.iys)
+                h[t] = (T)beam_current(jr.beam, k, vt);
+            else
+                h[t] = (T)__dmul_rn(jr.sig[t], (double)Ez[jr.base[l] + g.sz * k]);
         }
     }
     wake_taps<T>(E, g, tp, n);

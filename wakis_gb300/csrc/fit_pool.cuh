@@ -32,11 +32,14 @@ struct PoolSlot {
     bool joined = false;          // the pool stream has waited on `ready`
     double t_submit = 0.0, t_start = -1.0;
     long long pre_steps = 0;  // steps taken at submission (the odd first step of a fused context)
+    bool cancel = false;      // fit_pool_cancel: no further chunks; reported once none is in flight
+    int inflight = 0;         // chunks in flight that step this context
 };
 
 struct InFlight {
     int buf = 0;
-    std::vector<PoolSlot*> finishing;
+    std::vector<PoolSlot*> members;    // every context the chunk steps
+    std::vector<PoolSlot*> finishing;  // those whose last steps it takes
     double t_launch = 0.0;
 };
 
@@ -123,6 +126,23 @@ void pool_abort(FitPool* p, cudaError_t e, const char* what) {
     for (PoolSlot* s : p->incoming) finish_slot(p, s, FIT_ERR_CUDA, t);
     p->incoming.clear();
     p->cv_done.notify_all();
+}
+
+// active contexts cancelled by fit_pool_cancel that no chunk in flight steps any more are
+// handed back with FIT_ERR_CANCELLED (caller holds p->mu)
+void retire_cancelled(FitPool* p, double t) {
+    bool any = false;
+    for (size_t i = 0; i < p->active.size();) {
+        PoolSlot* s = p->active[i];
+        if (s->cancel && s->inflight == 0) {
+            p->active.erase(p->active.begin() + i);
+            finish_slot(p, s, FIT_ERR_CANCELLED, t);
+            any = true;
+        } else {
+            ++i;
+        }
+    }
+    if (any) p->cv_done.notify_all();
 }
 
 // fills pinned table `b` with the members that still have steps to enqueue, ordered by
@@ -280,12 +300,13 @@ void pool_main(FitPool* p) {
                 continue;
             }
             if (!p->stop) {
+                retire_cancelled(p, p->now());
                 while (!p->incoming.empty() && (int)p->active.size() < kPoolMaxInst) {
                     p->active.push_back(p->incoming.front());
                     p->incoming.pop_front();
                 }
                 for (PoolSlot* s : p->active)
-                    if (s->sched < s->nsteps) members.push_back(s);
+                    if (s->sched < s->nsteps && !s->cancel) members.push_back(s);
                 launch = !members.empty() && fl.size() < 2;
                 for (int c = 0; c < 3; ++c) {
                     tune.minb[c] = p->minb[c];
@@ -322,13 +343,18 @@ void pool_main(FitPool* p) {
             f.t_launch = p->now();
             if (busy_since < 0) busy_since = f.t_launch;
             long long cells = 0;
-            for (PoolSlot* s : members) {
-                const long long take = std::min<long long>(p->chunk, s->nsteps - s->sched);
-                if (s->t_start < 0) s->t_start = f.t_launch;
-                s->sched += take;
-                cells += take * s->c->g.N;
-                if (s->sched >= s->nsteps) f.finishing.push_back(s);
+            {
+                std::lock_guard<std::mutex> lk(p->mu);  // inflight is read by retire_cancelled
+                for (PoolSlot* s : members) {
+                    const long long take = std::min<long long>(p->chunk, s->nsteps - s->sched);
+                    if (s->t_start < 0) s->t_start = f.t_launch;
+                    s->sched += take;
+                    s->inflight++;
+                    cells += take * s->c->g.N;
+                    if (s->sched >= s->nsteps) f.finishing.push_back(s);
+                }
             }
+            f.members = members;
             {
                 std::lock_guard<std::mutex> lk(p->mu);
                 p->chunks++;
@@ -354,11 +380,13 @@ void pool_main(FitPool* p) {
             p->busy_ms += t - busy_since;
             busy_since = -1.0;
         }
+        for (PoolSlot* s : f.members) s->inflight--;
         for (PoolSlot* s : f.finishing) {
             p->active.erase(std::remove(p->active.begin(), p->active.end(), s), p->active.end());
             finish_slot(p, s, FIT_OK, t);
         }
         if (!f.finishing.empty()) p->cv_done.notify_all();
+        retire_cancelled(p, t);
     }
     // stopping: what is still in the pool is handed back unfinished
     std::lock_guard<std::mutex> lk(p->mu);
@@ -568,6 +596,29 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     }
     p->cv_work.notify_all();
     return FIT_OK;
+}
+
+int fit_pool_cancel(FitPool* p, int64_t tag) {
+    if (!p) return FIT_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    for (auto it = p->incoming.begin(); it != p->incoming.end(); ++it) {
+        if ((*it)->tag == tag) {
+            PoolSlot* s = *it;
+            p->incoming.erase(it);
+            finish_slot(p, s, FIT_ERR_CANCELLED, p->now());
+            p->cv_done.notify_all();
+            return FIT_OK;
+        }
+    }
+    for (PoolSlot* s : p->active) {
+        if (s->tag == tag) {  // a repeated cancel is a no-op
+            s->cancel = true;
+            p->cv_work.notify_all();
+            return FIT_OK;
+        }
+    }
+    p->err = "fit_pool_cancel: no queued or running solve with tag " + std::to_string((long long)tag);
+    return FIT_ERR_ARG;
 }
 
 int fit_pool_poll(FitPool* p, FitPoolDone* out, int32_t max, int32_t wait_ms) {

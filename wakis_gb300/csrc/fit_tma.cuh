@@ -23,9 +23,9 @@
 // are the same values and the results the same bits as k_step_fused and the two-pass
 // kernels (the same hpass_cells / epass_curl / epass_update code computes them).
 //
-// Waits are bounded (kWaitLimit polls): a CTA whose copies do not arrive records
-// FIT_ERR_TIMEOUT in *err, stops storing, waits (bounded) for the copies it issued and
-// returns.  No cluster multicast is used: every copy reads this GPU's own buffers.
+// Waits are bounded (wlim polls): a CTA whose copies do not arrive records
+// FIT_ERR_TIMEOUT in *err, stops storing, waits (bounded by kWaitLimit) for the copies it
+// issued and returns.  No cluster multicast is used: every copy reads this GPU's own buffers.
 #pragma once
 #include <cuda.h>
 
@@ -49,6 +49,17 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
         "[%5];" ::"r"(smem_u32(dst)),
         "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
+}
+// the same boxes requested into L2 only (no shared memory, no completion to wait for)
+__device__ __forceinline__ void tma_prefetch_4d(const CUtensorMap* map, int x, int y, int z, int c) {
+    asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(map), "r"(x), "r"(y),
+                 "r"(z), "r"(c)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, int y, int z) {
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(map), "r"(x), "r"(y),
+                 "r"(z)
+                 : "memory");
 }
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
@@ -74,8 +85,14 @@ struct TmaLayout {
     static constexpr size_t OFF_E = 0;
     static constexpr size_t OFF_H = OFF_E + NE * E_SLOT;
     static constexpr size_t OFF_C = OFF_H + NH * H_SLOT;
-    static constexpr size_t OFF_F = OFF_C + NH * C_SLOT;  // FusedShared (new H planes)
-    static constexpr size_t OFF_B = r128(OFF_F + sizeof(FusedShared<T, VEC, FY>));
+    // new H handed between warps: rb[2][Hx, Hz][row][x] -- the row below warp r's row
+    // (row 0: the halo warp's row y0-1; row r: warp r-1's row) -- and xb[2][Hy, Hz][row],
+    // the cell before each row segment; [2]: ping-pong by plane parity
+    static constexpr size_t RB_BYTES = 2u * 2u * FY * FX * sizeof(T);
+    static constexpr size_t XB_BYTES = 2u * 2u * FY * sizeof(T);
+    static constexpr size_t OFF_R = OFF_C + NH * C_SLOT;
+    static constexpr size_t OFF_X = OFF_R + RB_BYTES;
+    static constexpr size_t OFF_B = r128(OFF_X + XB_BYTES);
     static constexpr size_t BYTES = OFF_B + (NE + NH) * sizeof(unsigned long long);
     static_assert(EW <= 256 && CW <= 256 && HR + 1 <= 256, "TMA box dimensions are at most 256");
     static_assert((EW * sizeof(T)) % 16 == 0 && (HW * sizeof(T)) % 16 == 0 && (CW * 2) % 16 == 0,
@@ -91,8 +108,8 @@ __device__ __forceinline__ void box_v(T (&r)[VEC], const T* row, int col) {
 
 // Row-warp / halo-row input gathering for the H update of the VEC cells (i0.., j, k) of
 // box row rE (E box) / rH (H and code boxes), box column col (of the first cell, E box
-// coordinates; H box column col, code box column col - A + 8).  yfb: the +y neighbour
-// row is outside the box (j = Ny-1: flat crossing), read from global memory.  The +x
+// coordinates; H box column col, code box column col - A + 8).  The +y neighbour of the
+// last row (j = Ny-1: the flat crossing into plane k+1) is read from global memory.  The +x
 // neighbour after the vector comes from the next lane (shuffle), lane 31 from the box,
 // or from global memory at the flat crossing (i0 + VEC = Nx).  Every lane of the warp
 // must call this (shuffles); off lanes compute on in-box zeros and store nothing.
@@ -166,20 +183,25 @@ __device__ __forceinline__ void tma_hpass_row(const T* __restrict__ Ek, const T*
 // The whole step on coded coefficients (MODE 0 lossless, 1 loss factor): (Ein, Hin) ->
 // (Eout, Hout) for the planes [blockIdx.z*zlen, +zlen) of tile column (blockIdx.x,
 // blockIdx.y).  tmE / tmH: 4-D maps (Nx, Ny, Nz, 3) of Ein / Hin; tmC: 3-D map of the codes.
+// A row warp keeps the new H_x, H_y of its own cells from one plane to the next (the
+// plane-below values of the E update); the row-below and cell-before values cross warps
+// through the rb / xb buffers, which alternate with the plane parity, so one barrier per
+// plane suffices.  MB: CTAs per SM the register budget is sized for.
 template <typename T, int VEC, int FY, int MB, int MODE, int NE, int NH>
 __global__ void __launch_bounds__(32 * (FY + 1), MB)
     k_step_tma(const __grid_constant__ CUtensorMap tmE, const __grid_constant__ CUtensorMap tmH,
                const __grid_constant__ CUtensorMap tmC, const T* __restrict__ Ein, const T* __restrict__ Hin,
                T* __restrict__ Eout, T* __restrict__ Hout, T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
                BeamArgs b, StepArgs st, int zlen, const unsigned short* __restrict__ code, const T* __restrict__ tab,
-               int* err) {
+               int* err, long long wlim, int pf) {
     using L = TmaLayout<T, VEC, FY, NE, NH>;
     constexpr int FX = L::FX, A = L::A, EW = L::EW, ER = L::ER, HR = L::HR, HW = L::HW, CW = L::CW;
     extern __shared__ __align__(128) unsigned char smem[];
     T* Ering = reinterpret_cast<T*>(smem + L::OFF_E);
     T* Hring = reinterpret_cast<T*>(smem + L::OFF_H);
     unsigned short* Cring = reinterpret_cast<unsigned short*>(smem + L::OFF_C);
-    FusedShared<T, VEC, FY>& sm = *reinterpret_cast<FusedShared<T, VEC, FY>*>(smem + L::OFF_F);
+    T(*rb)[2][FY][FX] = reinterpret_cast<T(*)[2][FY][FX]>(smem + L::OFF_R);
+    T(*xb)[2][FY] = reinterpret_cast<T(*)[2][FY]>(smem + L::OFF_X);
     unsigned long long* barE = reinterpret_cast<unsigned long long*>(smem + L::OFF_B);
     unsigned long long* barH = barE + NE;
 
@@ -226,27 +248,31 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
         e_issued = min(e_last, k0 + NE - 2);
         for (int p = k0; p <= min(k1 - 1, k0 + NH - 2); ++p) issue_h(p);
         h_issued = min(k1 - 1, k0 + NH - 2);
-    }
-    // the new H of plane k0-1 (the plane below the range) for the tile, from global memory
-    if (k0 > 0 && !halo && on) {
-        T hx[VEC], hy[VEC], hz[VEC];
-        const long long n = (long long)i0 + g.sy * j + g.sz * (k0 - 1);
-        hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, mt, n, i0, j, k0 - 1, hx, hy, hz, code, tab);
-        const int bp = (k0 - 1) % 3;
-#pragma unroll
-        for (int e = 0; e < VEC; ++e) {
-            sm.h[bp][0][ty + 1][xo + e] = hx[e];
-            sm.h[bp][1][ty + 1][xo + e] = hy[e];
-            sm.h[bp][2][ty + 1][xo + e] = hz[e];
+        // L2 prefetch of the planes the next pf ring loads will read
+        for (int p = e_issued + 1; p <= min(e_last, e_issued + pf); ++p) tma_prefetch_4d(&tmE, x0 - A, y0 - 1, p, 0);
+        for (int p = h_issued + 1; p <= min(k1 - 1, h_issued + pf); ++p) {
+            tma_prefetch_4d(&tmH, x0 - A, y0 - 1, p, 0);
+            tma_prefetch_3d(&tmC, x0 - 8, y0 - 1, p);
         }
     }
-    bool ok = mbar_wait(&barE[0], 0u, kWaitLimit);  // plane k0 of E
-    int kdone = k0;                                  // planes [k0, kdone) completed
+    // the new H_x, H_y of the thread's cells one plane below (zero below plane 0); for a
+    // range starting at k0 > 0, plane k0-1 computed from global memory (the CTA below
+    // stores it)
+    T px[VEC], py[VEC];
+    zero_v<T, VEC>(px);
+    zero_v<T, VEC>(py);
+    if (k0 > 0 && !halo && on) {
+        T hz[VEC];
+        const long long n = (long long)i0 + g.sy * j + g.sz * (k0 - 1);
+        hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, mt, n, i0, j, k0 - 1, px, py, hz, code, tab);
+    }
+    bool ok = mbar_wait(&barE[0], 0u, wlim);  // plane k0 of E
+    int kdone = k0;                            // planes [k0, kdone) completed
     for (int k = k0; k < k1; ++k) {
-        const int bc = k % 3, bp = (k + 2) % 3;
+        const int bc = k & 1;
         if (k + 1 <= e_last)
-            ok = ok && mbar_wait(&barE[(k + 1 - k0) % NE], (unsigned)(((k + 1 - k0) / NE) & 1), kWaitLimit);
-        ok = ok && mbar_wait(&barH[(k - k0) % NH], (unsigned)(((k - k0) / NH) & 1), kWaitLimit);
+            ok = ok && mbar_wait(&barE[(k + 1 - k0) % NE], (unsigned)(((k + 1 - k0) / NE) & 1), wlim);
+        ok = ok && mbar_wait(&barH[(k - k0) % NH], (unsigned)(((k - k0) / NH) & 1), wlim);
         const T* Ek = eslot(k);
         const T* Ek1 = eslot(k + 1);
         const T* Hk = hslot(k);
@@ -263,11 +289,9 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
                     st_v<T, VEC>(Hout + g.N + n, hy);
                     st_v<T, VEC>(Hout + 2 * g.N + n, hz);
                 }
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) {
-                    sm.h[bc][0][ty + 1][xo + e] = hx[e];
-                    sm.h[bc][1][ty + 1][xo + e] = hy[e];
-                    sm.h[bc][2][ty + 1][xo + e] = hz[e];
+                if (ty + 1 < FY) {  // the row below of warp ty+1
+                    st_v<T, VEC>(&rb[bc][0][ty + 1][xo], hx);
+                    st_v<T, VEC>(&rb[bc][1][ty + 1][xo], hz);
                 }
             }
         } else {
@@ -277,11 +301,8 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
                 unsigned cq[VEC];
                 tma_hpass_row<T, VEC, FY, NE, NH>(Ek, Ek1, Hk, Ck, 0, 0, A + xo, Ein, g, mt, tab, n, i0, j, k, lane,
                                                   ax, ay, az, cq);
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) {
-                    sm.h[bc][0][0][xo + e] = ax[e];
-                    sm.h[bc][2][0][xo + e] = az[e];
-                }
+                st_v<T, VEC>(&rb[bc][0][0][xo], ax);
+                st_v<T, VEC>(&rb[bc][1][0][xo], az);
             } else if (i0 < g.nx) {  // y0 = 0: wraps to (i, Ny-1, k-1)
                 T ax[VEC], ay[VEC], az[VEC];
                 const long long m = (long long)i0 + g.sz * k - g.sy;
@@ -293,11 +314,8 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
                     zero_v<T, VEC>(ax);
                     zero_v<T, VEC>(az);
                 }
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) {
-                    sm.h[bc][0][0][xo + e] = ax[e];
-                    sm.h[bc][2][0][xo + e] = az[e];
-                }
+                st_v<T, VEC>(&rb[bc][0][0][xo], ax);
+                st_v<T, VEC>(&rb[bc][1][0][xo], az);
             }
             // the cell before each row segment: flat n - 1
             const int jj = y0 + lane;
@@ -341,12 +359,13 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
                     ay[0] = T(0);
                     az[0] = T(0);
                 }
-                sm.hx1[bc][0][lane + 1] = ay[0];
-                sm.hx1[bc][1][lane + 1] = az[0];
+                xb[bc][0][lane] = ay[0];
+                xb[bc][1][lane] = az[0];
             }
         }
-        // every thread is past plane k-1 (its slots are free) and the new H of plane k is
-        // in sm; the give-up decision is CTA-uniform
+        // every thread is past plane k-1 (its ring slots and the rb / xb buffers of plane
+        // k+1's parity are free) and the new H of plane k is in rb / xb; the give-up
+        // decision is CTA-uniform
         ok = __syncthreads_and(ok);
         if (!ok) break;
         kdone = k + 1;
@@ -354,32 +373,25 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
             fence_proxy_async();
             if (e_issued < e_last && e_issued + 1 <= k + NE - 1) issue_e(++e_issued);
             if (h_issued < k1 - 1 && h_issued + 1 <= k + NH - 1) issue_h(++h_issued);
+            // keep the L2 prefetch pf planes ahead of the ring loads
+            if (pf > 0 && e_issued + pf <= e_last) tma_prefetch_4d(&tmE, x0 - A, y0 - 1, e_issued + pf, 0);
+            if (pf > 0 && h_issued + pf <= k1 - 1) {
+                tma_prefetch_4d(&tmH, x0 - A, y0 - 1, h_issued + pf, 0);
+                tma_prefetch_3d(&tmC, x0 - 8, y0 - 1, h_issued + pf);
+            }
         }
         if (!halo && j < g.ny) {
-            T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
-#pragma unroll
-            for (int e = 0; e < VEC; ++e) {
-                hxy[e] = sm.h[bc][0][ty][xo + e];
-                hzy[e] = sm.h[bc][2][ty][xo + e];
-            }
-            if (k > 0) {
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) {
-                    hxz[e] = sm.h[bp][0][ty + 1][xo + e];
-                    hyz[e] = sm.h[bp][1][ty + 1][xo + e];
-                }
-            } else {
-                zero_v<T, VEC>(hxz);
-                zero_v<T, VEC>(hyz);
-            }
+            T hxy[VEC], hzy[VEC];
+            ld_v<T, VEC>(hxy, &rb[bc][0][ty][xo]);
+            ld_v<T, VEC>(hzy, &rb[bc][1][ty][xo]);
             T hyx = __shfl_up_sync(0xffffffffu, hy[VEC - 1], 1);
             T hzx = __shfl_up_sync(0xffffffffu, hz[VEC - 1], 1);
             if (lane == 0) {
-                hyx = sm.hx1[bc][0][ty + 1];
-                hzx = sm.hx1[bc][1][ty + 1];
+                hyx = xb[bc][0][ty];
+                hzx = xb[bc][1][ty];
             }
             T cur[3][VEC];
-            epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
+            epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, px, py, hyx, hzx, cur, i0, j, k, g, mt);
             T kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
             tab_get_v<T, VEC>(tab, cd, 1, kx, ky, kz);
             if constexpr (MODE == 1) {
@@ -399,6 +411,11 @@ __global__ void __launch_bounds__(32 * (FY + 1), MB)
                 st_v<T, VEC>(Eout + n, ex);
                 st_v<T, VEC>(Eout + g.N + n, ey);
                 st_v<T, VEC>(Eout + 2 * g.N + n, ez);
+            }
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                px[e] = hx[e];
+                py[e] = hy[e];
             }
         }
     }

@@ -67,10 +67,13 @@ class GridFIT3D:
                              "  - Provide grid axis arrays: x, y, z\n"
                              "  - OR domain extents and number of cells: xmin, xmax, ymin, ymax, zmin, zmax, "
                              "Nx, Ny, Nz\n  - OR load from a file using load_from_h5")
+        self.use_mesh_refinement = use_mesh_refinement
+        self.refinement_method = refinement_method
+        self.snap_points = snap_points
+        self.snap_tol = snap_tol
+        self.snap_solids = snap_solids
         if use_mesh_refinement:
-            raise NotImplementedError("use_mesh_refinement snaps the mesh to STL features, which needs VTK; "
-                                      "pass refined x, y, z arrays instead")
-        self.use_mesh_refinement = False
+            self._refine_from_snaps(snap_points, stl_solids, refinement_method, refinement_tol)
         self.dx, self.dy, self.dz = np.diff(self.x), np.diff(self.y), np.diff(self.z)
         self.update_logger(["Nx", "Ny", "Nz", "dx", "dy", "dz"])
         self.update_logger(["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"])
@@ -89,6 +92,72 @@ class GridFIT3D:
         self.update_logger(["gridInitializationTime"])
 
     # ------------------------------------------------------------------ metrics
+    # ------------------------------------------------------------------ mesh refinement
+    def _refine_from_snaps(self, snap_points, stl_solids, method, tol):
+        """use_mesh_refinement (wakis/gridFIT3D.py:204-217, 654-699, 861-920): each axis is
+        re-spaced by refine_axis so that it passes through the snap coordinates.  The
+        reference derives those from the STL solids' feature edges (points lying in the
+        x = 0, y = 0 and z = 0 planes, rounded to 5 decimals, plus the domain bounds),
+        which needs VTK: that extraction is not provided.  Given snap_points (an (n, 3)
+        array standing for those edge points), the same derivation runs on them; the
+        reference itself raises AttributeError there, as it reads x_snaps, which only the
+        STL extraction sets."""
+        if snap_points is None:
+            if stl_solids is not None:
+                raise NotImplementedError("use_mesh_refinement extracts snap points from STL feature edges, which "
+                                          "needs VTK; pass snap_points, or refined x, y, z arrays")
+            raise AttributeError("'GridFIT3D' object has no attribute 'x_snaps'")
+        pts = np.atleast_2d(np.asarray(snap_points, dtype=float))
+        for a, name in enumerate("xyz"):
+            lo, hi = getattr(self, name + "min"), getattr(self, name + "max")
+            snaps = np.unique(np.concatenate(([lo], np.unique(np.round(pts[:, a], 5)), [hi])))
+            setattr(self, name + "_snaps", snaps)
+        self.x = self.refine_axis(self.xmin, self.xmax, self.Nx + 1, self.x_snaps, method=method, tol=tol)
+        self.y = self.refine_axis(self.ymin, self.ymax, self.Ny + 1, self.y_snaps, method=method, tol=tol)
+        self.z = self.refine_axis(self.zmin, self.zmax, self.Nz + 1, self.z_snaps, method=method, tol=tol)
+        self.Nx, self.Ny, self.Nz = len(self.x) - 1, len(self.y) - 1, len(self.z) - 1
+
+    @staticmethod
+    def _spread_residuals(u, anchor, pinned):
+        """The three residuals refine_axis minimises over the normalised node positions u
+        (wakis/gridFIT3D.py:795-808): pinned nodes that moved (weight 1000, squared), gaps
+        below the uniform gap 1/(n-1) (squared shortfall), and 10 x the standard deviation
+        of the gaps."""
+        gaps = np.diff(u)
+        moved = np.sum((u[pinned] - anchor[pinned]) ** 2) * 1000
+        small = gaps[gaps < 1 / (len(u) - 1)]
+        short = np.sum((1 / (len(u) - 1) - small) ** 2)
+        return np.hstack([moved, short, np.std(gaps) * 10])
+
+    def refine_axis(self, xmin, xmax, Nx, x_snaps, method="insert", tol=1e-12):
+        """Nodes of an axis on [xmin, xmax] that pass through the snap coordinates x_snaps with
+        gaps as even as possible (wakis/gridFIT3D.py:771-859).  Positions are normalised
+        to [0, 1] and a start is built: 'insert' merges the snaps into Nx - len(x_snaps)
+        uniform nodes; 'neighbor' moves, for each snap, the first of Nx uniform nodes
+        within half a gap onto it.  Then scipy's least_squares (dogbox within [0, 1],
+        arctan loss, 3-point Jacobian, tolerances tol) minimises _spread_residuals, which
+        keeps the snap nodes in place.  'subdivision' raises the reference's
+        UnboundLocalError (its start is never assigned); other names raise ValueError."""
+        from scipy.optimize import least_squares
+        snaps = (x_snaps - xmin) / (xmax - xmin)
+        if method == "insert":
+            start = np.unique(np.append(snaps, np.linspace(0, 1, Nx - len(snaps))))
+        elif method == "neighbor":
+            start = np.linspace(0, 1, Nx)
+            half = np.diff(start)[0] / 2
+            for v in snaps:
+                near = np.isclose(start, v, rtol=0.0, atol=half)
+                if near.any():
+                    start[np.argmax(near)] = v
+        elif method == "subdivision":
+            raise UnboundLocalError("cannot access local variable 'x' where it is not associated with a value")
+        else:
+            raise ValueError(f"Method {method} not supported. Use 'insert', 'neighbor' or 'subdivision'.")
+        pinned = np.isin(start, snaps)
+        fit = least_squares(self._spread_residuals, x0=start.copy(), bounds=(0, 1), jac="3-point", method="dogbox",
+                            loss="arctan", gtol=tol, ftol=tol, xtol=tol, verbose=0, args=(start.copy(), pinned.copy()))
+        return fit.x * (xmax - xmin) + xmin
+
     def _compute_grid(self):
         self.grid = _MaskStore()
         tx = np.append((self.x[1:] + self.x[:-1]) / 2, 0.0)

@@ -36,21 +36,18 @@ class RoutinesMixin:
         self.Nt = Nt
         if source is not None:
             self.source = source
+        if save:
+            self._open_saves(fields, components)
         if plot or plot3d:
             raise NotImplementedError("plotting is not provided")
-        hfs = None
-        if save:
-            hfs = self._open_saves(Nt, fields, components, save_every, subdomain)
         abc_axes = self._abc_lo_axes() if self.activate_abc else 0
         self._ctx.call("fit_set_abc", abc_axes)
         # J = sigma*E is taken at the end of the step, before the ABC copy changes plane 0,
         # so on a conductive grid J stays explicit while ABC faces are updated
         self._force_explicit = bool(abc_axes) and self.use_conductivity
         try:
-            fast = (callback is None and not save and type(source) in (PlaneWave, WavePacket)
-                    and not self._force_explicit)
-            free = (source is None and callback is None and not save and not self._force_explicit
-                    and self._beam is None)
+            fast = callback is None and type(source) in (PlaneWave, WavePacket) and not self._force_explicit
+            free = source is None and callback is None and not self._force_explicit and self._beam is None
             if fast and Nt > 0:
                 self._emsolve_device(Nt, source)
             elif free and Nt > 0:
@@ -59,8 +56,6 @@ class RoutinesMixin:
                 for n in range(Nt):
                     if source is not None:
                         source.update(self, n * self.dt)
-                    if save and n % save_every == 0:
-                        self._save_step(hfs, n)
                     self.one_step()
                     if callback is not None:
                         callback(self, n * self.dt)
@@ -70,8 +65,6 @@ class RoutinesMixin:
                 # J holds sigma*E of the pre-ABC planes: it stays the truth for the next step
                 self._j_state, self._j_zero, self._j_stale = "tensor", False, False
             self._force_explicit = False
-            if hfs is not None:
-                self._close_saves(hfs)
 
     def _emsolve_free(self, Nt):
         """emsolve without a source or callback: the first step through the host path
@@ -134,10 +127,10 @@ class RoutinesMixin:
         reference always writes to Ez.h5 is recorded on the device only with save_Ez=True
         and written to wake.Ez_file at the end (HDF5 with the reference's datasets when
         h5py is importable, else an .npz archive with the same keys); the wake potential
-        itself comes from the device taps either way.  save_J writes the J_z slabs on the
-        same lines, taken after the beam update and before each step, to Jz.h5 (Jz.npz
-        without h5py) in the working directory, as the reference does; the steps then run
-        one by one from the host, as a callback makes them."""
+        itself comes from the device taps either way.  save_J records the J_z slabs on the
+        same lines on the device, taken after the beam update and before each step, and
+        writes them to Jz.h5 (Jz.npz without h5py) in the working directory, as the
+        reference does."""
         if wake is not None:
             self.wake = wake
         if self.wake is None:
@@ -151,16 +144,12 @@ class RoutinesMixin:
         wake = self.wake
         beam, Nt = self._wake_prepare(wake, wakelength, compute_plane)
         hist = self._start_ez_record(wake, Nt) if save_Ez and Nt > 0 else None
+        jhist = self._start_jz_record(wake, Nt) if save_J and Nt > 0 else None
         if self.verbose:
             print("Running electromagnetic time-domain simulation...")
         t0 = time.time()
         monitor = field_monitor if (use_field_monitor and field_monitor is not None) else None
-        fast = callback is None and not save_J and (monitor is None or isinstance(monitor, FieldMonitor))
-        jslabs = [] if save_J else None
-        if compute_plane.lower() == "longitudinal":
-            xx, yy = self.ixt, self.iyt
-        else:
-            xx, yy = slice(self.ixt - 1, self.ixt + 2), slice(self.iyt - 1, self.iyt + 2)
+        fast = callback is None and (monitor is None or isinstance(monitor, FieldMonitor))
         if fast and Nt > 0:
             vt = self._wake_device_setup(beam, Nt)
             first = self._wake_first_step(beam)
@@ -179,8 +168,6 @@ class RoutinesMixin:
         else:
             for n in range(Nt):
                 beam.update(self, n * self.dt)
-                if jslabs is not None:
-                    jslabs.append(self.J[xx, yy, :, "z"])
                 self._advance(n)
                 if use_field_monitor and field_monitor is not None:
                     field_monitor.update(self.E, self.dt)
@@ -190,8 +177,9 @@ class RoutinesMixin:
         if hist is not None:
             self._ctx.call("fit_set_ez_record", None, 0, None, None, 0, 0)
             self._write_ez(wake, hist, Nt)
-        if jslabs is not None:
-            self._write_history("Jz.h5", wake, jslabs)
+        if jhist is not None:
+            self._ctx.call("fit_set_jz_record", None, 0, None, None, 0, 0, None)
+            self._write_lines("Jz.h5", wake, jhist, Nt)
         wake.solve(compute_plane=compute_plane)
         self.logger.wakeSolver = wake.logger.wakeSolver
         self.logger.wakeSolver["wakelength"] = wakelength
@@ -262,11 +250,30 @@ class RoutinesMixin:
                        nat.iptr32(ly), 0, int(Nt))
         return hist
 
-    def _write_ez(self, wake, hist, Nt):
-        """Ez.h5 of the reference from the device-recorded history (Nt, lines, Nz)."""
+    def _start_jz_record(self, wake, Nt):
+        """Device buffer (Nt, lines, Nz) of J_z on the wake's lines, filled by the step
+        prologue after the beam update and before every step (the reference's save_J dump,
+        wakis/routines.py:440-445): the beam current on the beam line, sigma*E elsewhere."""
+        lines = wake._run["lines"]
+        hist = torch.empty((Nt, len(lines), self.Nz), dtype=self.E.array.dtype, device=self.E.array.device)
+        lx = np.ascontiguousarray([l[0] for l in lines], dtype=np.int32)
+        ly = np.ascontiguousarray([l[1] for l in lines], dtype=np.int32)
+        sz = self.sigma.to_matrix(2)
+        sig = np.ascontiguousarray(torch.stack([sz[int(a), int(b), :] for a, b in lines]).double().cpu().numpy())
+        self._ctx.call("fit_set_jz_record", nat.C.c_void_p(hist.data_ptr()), len(lines), nat.iptr32(lx),
+                       nat.iptr32(ly), 0, int(Nt), nat.dptr(sig))
+        return hist
+
+    def _write_lines(self, fname, wake, hist, Nt):
+        """A line-history file (Ez.h5, Jz.h5) of the reference from a device-recorded history
+        (Nt, lines, Nz); returns the name written."""
         slabs = hist.cpu().numpy()
         shape = (3, 3, self.Nz) if slabs.shape[1] == 9 else (self.Nz,)
-        wake.Ez_file = self._write_history(wake.Ez_file, wake, [slabs[n].reshape(shape) for n in range(Nt)])
+        return self._write_history(fname, wake, [slabs[n].reshape(shape) for n in range(Nt)])
+
+    def _write_ez(self, wake, hist, Nt):
+        """Ez.h5 of the reference from the device-recorded history (Nt, lines, Nz)."""
+        wake.Ez_file = self._write_lines(wake.Ez_file, wake, hist, Nt)
 
     def _write_history(self, fname, wake, slabs):
         """A line-history file with the reference's datasets (wakis/routines.py:399-427):
@@ -323,34 +330,21 @@ class RoutinesMixin:
             self._j_stale = True
         self._e_zero = False
 
-    def _open_saves(self, Nt, fields, components, save_every, subdomain):
+    def _open_saves(self, fields, components):
+        """emsolve(save=True) as the reference runs it (wakis/routines.py:122-146): one HDF5
+        file per field and component, 'EAbs.h5', 'Ez.h5', 'Hy.h5', ..., opened for writing;
+        then the reference's loop that writes the grid datasets iterates over the file
+        NAMES (its dict's keys) and fails on the first one with TypeError, before any
+        step.  The same files are created (when h5py is importable) and the same exception
+        is raised."""
         try:
             import h5py
         except ImportError:
             h5py = None
-        hfs = {}
+        names = []
         for field in fields:
-            names = [field + c for c in components] if len(field) == 1 else [field]
+            names += [field + c for c in components] if len(field) == 1 else [field]
+        if h5py is not None:
             for nm in names:
-                hfs[nm] = {} if h5py is None else h5py.File(nm + ".h5", "w")
-        meta = dict(x=self.x, y=self.y, z=self.z, dx=self.grid.dx, dy=self.grid.dy, dz=self.grid.dz,
-                    t=np.arange(0, Nt * self.dt, save_every * self.dt))
-        for hf in hfs.values():
-            for k, v in meta.items():
-                hf[k] = v
-        self._save_sub = subdomain if subdomain is not None else (slice(0, self.Nx), slice(0, self.Ny),
-                                                                  slice(0, self.Nz))
-        self._save_h5 = h5py is not None
-        return hfs
-
-    def _save_step(self, hfs, n):
-        xx, yy, zz = self._save_sub
-        for name, hf in hfs.items():
-            hf["#" + str(n).zfill(5)] = getattr(self, name[0])[xx, yy, zz, name[1:]]
-
-    def _close_saves(self, hfs):
-        for name, hf in hfs.items():
-            if self._save_h5:
-                hf.close()
-            else:
-                np.savez(name + ".npz", **hf)
+                h5py.File(nm + ".h5", "w").close()
+        raise TypeError("'str' object does not support item assignment")

@@ -313,10 +313,19 @@ class ServingLoop:
     Admission is first-fit in arrival order: a request that fits the free budget is
     admitted even when an earlier one does not, unless the oldest waiting request has
     already been passed over ``max_bypass`` times, after which admission is strict FIFO
-    until it gets in (bounded waiting for large requests)."""
+    until it gets in (bounded waiting for large requests).
+
+    A failure ends one request, never the loop: a request whose footprint exceeds the
+    whole budget is rejected on arrival, one whose solver cannot be built (out of memory,
+    a library error) fails at admission, one cancelled while queued or running
+    (``cancel``) is handed back by the pool, and one whose wake potential or impedance is
+    not finite when read back fails at completion.  Each ends as a record with a status
+    ('done', 'rejected', 'failed', 'cancelled') and a reason; the others run on.  With
+    ``trace_path`` every record is also appended to that file as one JSON line."""
 
     def __init__(self, budget_bytes, chunk_steps=64, ctas_per_sm=0, device=0, dtype=np.float32, max_bypass=8,
-                 keep_results=True, variants=None, kernels="direct"):
+                 keep_results=True, variants=None, kernels="direct", trace_path=None):
+        self.budget = int(budget_bytes)
         self.pool = nat.Pool(budget_bytes, chunk_steps=chunk_steps, ctas_per_sm=ctas_per_sm, device=device)
         for vec, minb in (variants or {}).items():
             self.pool.tune(vec, minb)
@@ -326,29 +335,74 @@ class ServingLoop:
         self.admission = Admission(max_bypass)
         self.keep_results = keep_results
         self.results = {}
+        self.trace_path = trace_path
+        self._cancel = set()
 
     def close(self):
         self.pool.close()
 
-    def run(self, requests, time_scale=1.0):
+    def cancel(self, tag):
+        """Cancels a request: before admission it is dropped from the queue, while it runs
+        the pool stops stepping it.  Takes effect in the loop's next iteration."""
+        self._cancel.add(tag)
+
+    def _trace(self, rec):
+        if self.trace_path:
+            import json
+            with open(self.trace_path, "a") as fh:
+                fh.write(json.dumps(rec) + "\n")
+
+    def run(self, requests, time_scale=1.0, on_tick=None, readback_hook=None):
         """Serves the requests (arrival times in seconds, scaled by time_scale) and returns
-        per-request records and a summary."""
+        per-request records and a summary of the completed ones.  on_tick(loop, now_s, running_tags)
+        runs once per loop iteration (a caller can cancel from it); readback_hook(tag,
+        result) may inspect or alter a finished request's host-side results before the
+        finiteness check."""
         tmp = tempfile.mkdtemp()
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         queue = []
         running = {}
         records = []
         t0 = time.perf_counter()
+        size = lambda r: footprint_bytes(r, self.dtype, self.kernels)
+
+        def record(req, status, reason="", **kw):
+            rec = dict(tag=req.tag, status=status, reason=reason, cells=req.cells, lossy=req.lossy,
+                       arrival_s=req.arrival * time_scale, end_s=time.perf_counter() - t0)
+            rec.update(kw)
+            records.append(rec)
+            self._trace(rec)
+
         while pending or queue or running:
             now = time.perf_counter() - t0
             while pending and pending[0].arrival * time_scale <= now:
-                queue.append(pending.popleft())
+                req = pending.popleft()
+                if size(req) > self.budget:
+                    record(req, "rejected", "footprint above the pool budget", footprint=size(req))
+                else:
+                    queue.append(req)
+            if on_tick is not None:
+                on_tick(self, now, sorted(running))
+            for req in [r for r in queue if r.tag in self._cancel]:
+                queue.remove(req)
+                self._cancel.discard(req.tag)
+                record(req, "cancelled", "cancelled before admission")
+            for tag in [t for t in running if t in self._cancel]:
+                self._cancel.discard(tag)
+                try:
+                    self.pool.cancel(tag)
+                except nat.FitError:  # it finished in the meantime; poll reports it
+                    pass
             admitted = False
-            for req, nbytes in self.admission.admit(queue, lambda r: footprint_bytes(r, self.dtype, self.kernels),
-                                                    self.pool.reserve):
+            for req, nbytes in self.admission.admit(queue, size, self.pool.reserve):
                 t_adm = time.perf_counter() - t0
-                job = ServedSolve(req, self.dtype, self.device, tmp, self.kernels)
-                job.submit(self.pool)
+                try:
+                    job = ServedSolve(req, self.dtype, self.device, tmp, self.kernels)
+                    job.submit(self.pool)
+                except (nat.FitError, RuntimeError) as e:  # a library error or torch's out-of-memory
+                    self.pool.release(nbytes)
+                    record(req, "failed", f"setup: {e}", admitted_s=t_adm, footprint=nbytes)
+                    continue
                 running[req.tag] = (job, nbytes, t_adm, time.perf_counter() - t0)
                 admitted = True
             if running:
@@ -360,27 +414,35 @@ class ServingLoop:
                     wait = 50
                 for d in self.pool.poll(wait_ms=wait):
                     job, nbytes, t_adm, t_sub = running.pop(d["tag"])
-                    if d["status"] != 0:
-                        raise nat.FitError(d["status"], f"pooled solve {d['tag']} failed")
-                    res = job.finish()
-                    t_done = time.perf_counter() - t0
                     req = job.req
-                    rec = dict(tag=req.tag, cells=req.cells, steps=job.Nt, lossy=req.lossy,
-                               arrival_s=req.arrival * time_scale, admitted_s=t_adm, submitted_s=t_sub,
-                               done_s=t_done, tti_s=t_done - req.arrival * time_scale,
-                               pool_ms=d["t_done_ms"] - d["t_submit_ms"], footprint=nbytes)
-                    records.append(rec)
-                    if self.keep_results:
-                        self.results[req.tag] = res
+                    times = dict(admitted_s=t_adm, submitted_s=t_sub, pool_submit_ms=d["t_submit_ms"],
+                                 pool_start_ms=d["t_start_ms"], pool_done_ms=d["t_done_ms"], footprint=nbytes)
+                    if d["status"] == nat.FIT_ERR_CANCELLED:
+                        record(req, "cancelled", "cancelled while running", **times)
+                    elif d["status"] != 0:
+                        record(req, "failed", f"pool status {d['status']}", **times)
+                    else:
+                        res = job.finish()
+                        if readback_hook is not None:
+                            readback_hook(req.tag, res)
+                        bad = [k for k in ("WP", "WPx", "WPy", "Z", "Zx", "Zy")
+                               if not np.all(np.isfinite(np.asarray(res[k])))]
+                        t_done = time.perf_counter() - t0
+                        if bad:
+                            record(req, "failed", "non-finite " + ", ".join(bad), steps=job.Nt, **times)
+                        else:
+                            record(req, "done", steps=job.Nt, done_s=t_done, tti_s=t_done - req.arrival * time_scale,
+                                   pool_ms=d["t_done_ms"] - d["t_submit_ms"], **times)
+                            if self.keep_results:
+                                self.results[req.tag] = res
                     job.close()
                     del job
                     self.pool.release(nbytes)
             elif pending and not queue:
                 time.sleep(max(0.0, pending[0].arrival * time_scale - (time.perf_counter() - t0)))
-            elif queue and not admitted:
-                raise RuntimeError("a waiting request can never be admitted (footprint above the budget)")
         makespan = time.perf_counter() - t0
-        out = summarize(records, makespan)
+        out = summarize([r for r in records if r["status"] == "done"], makespan)
+        out["failed"] = {st: sum(r["status"] == st for r in records) for st in ("rejected", "failed", "cancelled")}
         out["pool"] = self.pool.stats()
         return records, out
 

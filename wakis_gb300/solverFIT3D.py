@@ -228,7 +228,7 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         fastest and remembers it for grids of the same shape (later calls reuse it unless
         force).  Staging 0 feeds the threads with per-thread loads; 1 and 2 with TMA plane
         rings (coded grids with Nx a multiple of 8 only; see fused_staging).
-        Returns {(vec, rows, zseg, ctas, staging): ms, 'two-pass': ms}."""
+        Returns {(vec, rows, zseg, ctas, staging, l2_ahead): ms, 'two-pass': ms}."""
         if self._kernels != "fused":
             self.kernels = "fused"
         key = self._grid_key()
@@ -243,7 +243,7 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self._ensure_codes()
         times = {}
         ms = np.zeros(2)
-        self._ctx.call("fit_set_fused_staging", 0)
+        self._ctx.call("fit_set_fused_staging", 0, 0)
         for vec in vecs:
             for rows, ctas in ((4, 3), (4, 4), (8, 2)):
                 for zseg in zsegs:
@@ -251,22 +251,23 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
                         continue
                     self._ctx.call("fit_set_fused_shape", vec, rows, zseg, ctas)
                     self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
-                    times[(vec, rows, zseg, ctas, 0)] = float(ms[0])
+                    times[(vec, rows, zseg, ctas, 0, 0)] = float(ms[0])
         two_pass = float(ms[1])
         if self._staging_candidates():
             vec = vecs[0]
             for rows, ctas, staging in ((4, 3, 1), (4, 3, 2), (8, 2, 1)):
-                for zseg in zsegs:
-                    if zseg > self.Nz:
-                        continue
-                    self._ctx.call("fit_set_fused_shape", vec, rows, zseg, ctas)
-                    try:
-                        self._ctx.call("fit_set_fused_staging", staging)
-                    except nat.FitError:
-                        break
-                    self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
-                    times[(vec, rows, zseg, ctas, staging)] = float(ms[0])
-            self._ctx.call("fit_set_fused_staging", 0)
+                for ahead in (1, 2):
+                    for zseg in zsegs:
+                        if zseg > self.Nz:
+                            continue
+                        self._ctx.call("fit_set_fused_shape", vec, rows, zseg, ctas)
+                        try:
+                            self._ctx.call("fit_set_fused_staging", staging, ahead)
+                        except nat.FitError:
+                            break
+                        self._ctx.call("fit_time_fused", int(reps), nat.dptr(ms))
+                        times[(vec, rows, zseg, ctas, staging, ahead)] = float(ms[0])
+            self._ctx.call("fit_set_fused_staging", 0, 0)
         times["two-pass"] = two_pass
         best = min((t for t in times if t != "two-pass"), key=times.get)
         SolverFIT3D._fused_shapes[key] = (best, times)
@@ -282,9 +283,10 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
     def fused_staging(self):
         """How the fused step's old fields reach the threads; the results are the same bit
         for bit.  'auto' (default): what the autotuner picked for this grid, else loads;
-        0: per-thread global loads; 1: tensor-memory-accelerator copies (cp.async.bulk.tensor)
-        of each plane's E, H and coefficient-code boxes into shared-memory rings 4 E planes
-        and 3 H planes deep; 2: 5 and 4 planes deep (as 1 with 8-row tiles).  Copies apply to coded
+        0: per-thread global loads; 1 or 2: tensor-memory-accelerator copies
+        (cp.async.bulk.tensor) of each plane's E, H and coefficient-code boxes into
+        shared-memory rings, sized for 3 (1) or 4 (2) CTAs per SM with 4-row tiles, with the
+        boxes of the next plane requested into L2 ahead of the ring loads.  Copies apply to coded
         grids with Nx a multiple of 8; elsewhere the step keeps the loads.  The
         environment variable WAKIS_GB300_STAGING sets the default."""
         return self._staging
@@ -300,22 +302,22 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         """Applies fused_staging to the context before a fused device loop."""
         if self._staging == "auto":
             hit = SolverFIT3D._fused_shapes.get(self._grid_key())
-            want = hit[0][4] if hit is not None else 0
+            want, ahead = (hit[0][4], hit[0][5]) if hit is not None else (0, 0)
         else:
-            want = int(self._staging)
+            want, ahead = int(self._staging), 1
         try:
-            self._ctx.call("fit_set_fused_staging", want)
+            self._ctx.call("fit_set_fused_staging", want, ahead)
         except nat.FitError:  # the grid does not qualify: loads
-            self._ctx.call("fit_set_fused_staging", 0)
+            self._ctx.call("fit_set_fused_staging", 0, 0)
 
     def _apply_tuned(self, best, times):
         """Sets the tuned fused shape and staging; under kernels='auto' a grid on which the
         two-pass step timed faster keeps the pass kernels."""
         self._ctx.call("fit_set_fused_shape", *best[:4])
         try:
-            self._ctx.call("fit_set_fused_staging", best[4] if len(best) > 4 else 0)
+            self._ctx.call("fit_set_fused_staging", *(best[4:6] if len(best) > 5 else (0, 0)))
         except nat.FitError:
-            self._ctx.call("fit_set_fused_staging", 0)
+            self._ctx.call("fit_set_fused_staging", 0, 0)
         if self._kernels_auto and times["two-pass"] < times[best]:
             self._ctx.call("fit_set_kernel_variant", 0)
             self._kernels = "direct"
@@ -543,6 +545,10 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         return state
 
     def load_state(self, filename="solver_state.h5"):
+        """Restores E, H, J from a file save_state wrote (wakis/solverFIT3D.py:959-996).  The
+        next step reads J as stored, as the reference does; when the stored J is zero, or is
+        exactly sigma*E as the device computes it, the solver keeps its folded-J step, whose
+        results are then those of an uninterrupted run bit for bit."""
         try:
             import h5py
             with h5py.File(filename, "r") as state:
@@ -553,6 +559,11 @@ class SolverFIT3D(RoutinesMixin, BCsMixin):
         self.E.fromarray(data["E"])
         self.H.fromarray(data["H"])
         self._J.fromarray(data["J"])
+        J, E = self._J.array, self.E.array
+        if not bool(torch.any(J != 0)):
+            self._j_state, self._j_zero, self._j_stale = "tensor", True, False
+        elif self.use_conductivity and torch.equal(J, self.sigma.array.to(J.dtype) * E):
+            self._j_state, self._j_zero, self._j_stale = "derived", False, False
 
     def read_state(self, filename="solver_state.h5"):
         try:
