@@ -320,6 +320,9 @@ typedef struct FitPoolStats {
     int32_t variant[3];     /* pass-kernel variant (CTAs per SM) for vector widths 4, 2, 1 */
     int32_t grid[3];        /* persistent CTAs of the E pass for vector widths 4, 2, 1 */
     double busy_ms;         /* host time with at least one chunk in flight */
+    int64_t fused_cell_updates;  /* the part of cell_updates taken by the fused kernel */
+    int32_t fused_variant[3];    /* fused kernel variant (CTAs per SM) for vector widths 4, 2, 1 */
+    int32_t fused_grid[3];       /* persistent CTAs of the fused kernel for vector widths 4, 2, 1 */
 } FitPoolStats;
 
 /* device: CUDA ordinal; budget_bytes > 0; chunk_steps in [1, 1024] (64 is a good
@@ -360,6 +363,11 @@ FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
  * defaults are 3, 3 and 4).  Applies from the next chunk; graphs of the old variant are recaptured.
  * The serving layer's autotuner times the variants on the requests' own grids. */
 FIT_API int fit_pool_tune(FitPool *pool, int32_t vec, int32_t ctas_per_sm);
+/* Chooses the variant of the pooled fused step for one vector-width class (vec = 4, 2
+ * or 1): ctas_per_sm 2 or 3 (the default) names the register budget it was compiled
+ * for.  Applies from the next chunk.  No counterpart in the reference (one solve per
+ * process there); the serving layer's autotuner calls it. */
+FIT_API int fit_pool_tune_fused(FitPool *pool, int32_t vec, int32_t ctas_per_sm);
 
 /* ---------------------------------------------------------------- field monitor
  * Running DFT of E at nf frequencies (FieldMonitor.update, wakis/field_monitors.py:59-101):

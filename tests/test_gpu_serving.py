@@ -188,3 +188,62 @@ def test_fused_pool_mix_with_odd_step_counts():
             a, b = np.asarray(got[k]), np.asarray(refs[j.req.tag][k])
             assert np.linalg.norm(a - b) <= 1e-5 * max(np.linalg.norm(b), 1e-30), (j.req.tag, k)
         j.close()
+
+
+def _run_pool(jobs, chunk_steps, variants=None):
+    pool = nat.Pool(8 << 30, chunk_steps=chunk_steps)
+    try:
+        for vec, minb in (variants or {}).items():
+            pool.tune_fused(vec, minb)
+        for j in jobs:
+            j.submit(pool)
+        done = []
+        while len(done) < len(jobs):
+            done += pool.poll(wait_ms=100)
+        stats = pool.stats()
+    finally:
+        pool.close()
+    assert all(d["status"] == 0 for d in done), done
+    return stats
+
+
+def test_fused_pool_equals_two_pass_wakesolve_bitwise(alone):
+    """The pool's fused step on plane segments, every vector width (Nx = 16 and 24:
+    4-wide, 18: 2-wide, 21: single cells), gives the two-pass wakesolve's results bit for
+    bit: the per-cell arithmetic is the same code, and the cells before a segment (the
+    previous plane's last row here, one segment per plane) are recomputed exactly."""
+    reqs = small_requests()
+    jobs = [S.ServedSolve(r, kernels="fused") for r in reqs]
+    stats = _run_pool(jobs, chunk_steps=8)
+    assert stats["fused_cell_updates"] == stats["cell_updates"] > 0
+    for j in jobs:
+        assert_same(j.finish(), alone[j.req.tag])
+        j.close()
+
+
+@pytest.mark.parametrize("minb", [2, 3])
+def test_fused_pool_multi_segment_planes_bitwise(minb):
+    """Planes of several segments (Nx*Ny = 2304 .. 2500 cells for 1024-cell segments, so
+    the cells before a segment are the previous segment's, in the same plane), both
+    compiled register budgets, a chunk length that ends solves inside a chunk: bit for bit
+    the two-pass wakesolve."""
+    reqs = [S.CavityRequest(tag=10, side=30e-3, rp=5e-3, n=48, sigmaz=8e-3, sigma=0.0, wakelength=0.02),
+            S.CavityRequest(tag=11, side=32e-3, rp=6e-3, n=50, sigmaz=9e-3, sigma=3e4, wakelength=0.02),
+            S.CavityRequest(tag=12, side=28e-3, rp=4e-3, n=49, sigmaz=7e-3, sigma=0.0, wakelength=0.02)]
+    refs = {r.tag: S.solve_alone(r, np.float32, kernels="direct") for r in reqs}
+    jobs = [S.ServedSolve(r, kernels="fused") for r in reqs]
+    stats = _run_pool(jobs, chunk_steps=10, variants={4: minb, 2: minb, 1: minb})
+    assert stats["fused_variant"] == {4: minb, 2: minb, 1: minb}
+    assert stats["fused_cell_updates"] == stats["cell_updates"]
+    for j in jobs:
+        assert_same(j.finish(), refs[j.req.tag])
+        j.close()
+
+
+def test_fused_pool_rejects_unknown_variant():
+    pool = nat.Pool(1 << 30, chunk_steps=8)
+    try:
+        with pytest.raises(nat.FitError):
+            pool.tune_fused(4, 5)
+    finally:
+        pool.close()

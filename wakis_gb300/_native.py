@@ -47,7 +47,8 @@ class FitPoolStats(C.Structure):
     _fields_ = [("chunks", C.c_int64), ("cell_updates", C.c_int64), ("budget_bytes", C.c_int64),
                 ("reserved_bytes", C.c_int64), ("active", C.c_int32), ("queued", C.c_int32),
                 ("max_active", C.c_int32), ("chunk_steps", C.c_int32), ("variant", C.c_int32 * 3),
-                ("grid", C.c_int32 * 3), ("busy_ms", C.c_double)]
+                ("grid", C.c_int32 * 3), ("busy_ms", C.c_double), ("fused_cell_updates", C.c_int64),
+                ("fused_variant", C.c_int32 * 3), ("fused_grid", C.c_int32 * 3)]
 
 
 _P = C.c_void_p
@@ -106,6 +107,7 @@ _SIGS = {
     "fit_pool_cancel": (_P, C.c_int64),
     "fit_pool_stats": (_P, C.POINTER(FitPoolStats)),
     "fit_pool_tune": (_P, C.c_int32, C.c_int32),
+    "fit_pool_tune_fused": (_P, C.c_int32, C.c_int32),
     "fit_version": (C.c_char_p, C.c_int64),
     "fit_launch_count": (),
 }
@@ -295,11 +297,17 @@ class Pool:
         out = {name: getattr(s, name) for name, _ in FitPoolStats._fields_}
         out["variant"] = {4: s.variant[0], 2: s.variant[1], 1: s.variant[2]}
         out["grid"] = {4: s.grid[0], 2: s.grid[1], 1: s.grid[2]}
+        out["fused_variant"] = {4: s.fused_variant[0], 2: s.fused_variant[1], 1: s.fused_variant[2]}
+        out["fused_grid"] = {4: s.fused_grid[0], 2: s.fused_grid[1], 1: s.fused_grid[2]}
         return out
 
     def tune(self, vec, ctas_per_sm):
         """Selects the compiled pass-kernel variant of one vector-width class."""
         self._check(self.lib.fit_pool_tune(self.h, int(vec), int(ctas_per_sm)))
+
+    def tune_fused(self, vec, ctas_per_sm):
+        """Selects the compiled variant of the pooled fused step of one vector-width class."""
+        self._check(self.lib.fit_pool_tune_fused(self.h, int(vec), int(ctas_per_sm)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -1908,14 +1908,16 @@ __global__ void k_dft_reduce(const double2* __restrict__ part, int nsig, int nb,
 // pooled instance gives bit-identical fields to the same grid run alone.
 constexpr int kPoolMaxInst = 64;
 constexpr int kPoolTpb = 256;
-// classes: 0, 1, 2 = two-pass kernels with 4-, 2-, 1-wide vectors; 3, 4 = the fused step
-// with 4- and 2-wide vectors (contexts with the fused step enabled and Nx even)
-constexpr int kPoolClasses = 5;
-constexpr int kPoolFusedRows = 4;   // rows per fused tile (plus the halo warp)
-constexpr int kPoolFusedZlen = 32;  // planes per fused work item
+// classes: 0, 1, 2 = two-pass kernels with 4-, 2-, 1-wide vectors; 3, 4, 5 = the fused
+// step on plane segments with 4-, 2-, 1-wide vectors (coded contexts with the fused step
+// enabled and Nx <= kSegMaxNx)
+constexpr int kPoolClasses = 6;
+constexpr int kSegTpb = 256;    // threads of a fused CTA
+constexpr int kSegCells = 1024; // cells of a plane segment (every vector width)
+constexpr int kSegMaxNx = 256;  // the fused class holds grids with Nx up to this
 
 __host__ __device__ constexpr int pool_class(int vec) { return vec == 4 ? 0 : (vec == 2 ? 1 : 2); }
-__host__ __device__ constexpr int pool_fused_class(int vec) { return vec == 4 ? 3 : 4; }
+__host__ __device__ constexpr int pool_fused_class(int vec) { return vec == 4 ? 3 : (vec == 2 ? 4 : 5); }
 
 template <typename T>
 struct PoolInst {
@@ -1934,17 +1936,17 @@ struct PoolInst {
     long long vt_len;
     long long n_end;  // steps n < n_end are taken
     long long tile0;  // first tile (fused: work item) of the instance in its class
-    long long ntile;  // tiles: ceil(nvec / kPoolTpb); fused: tiles_x * tiles_y * z ranges
+    long long ntile;  // tiles: ceil(nvec / kPoolTpb); fused: nseg * z ranges
     long long nvec;   // N / vec
     T* E2;            // fused: the second field buffers (steps alternate E,H <-> E2,H2)
     T* H2;
     int vec;          // cells per vector: 4, 2 or 1 (Nx % vec == 0)
     int mode;         // 0: lossless, 1: J = sigma*E folded into the loss factor
     int use_cond;
-    int fused;        // 1: stepped by k_step_fused_pool
-    int tiles_x, tiles_y;  // fused tile grid of one z range
-    int pad0, pad1;
-    const unsigned short* code;  // coded coefficients of the two-pass classes (nullptr: dense)
+    int fused;        // 1: stepped by k_step_seg_pool
+    int zlen;         // fused: planes per work item
+    long long nseg;   // fused: plane segments, ceil(Nx*Ny / kSegCells)
+    const unsigned short* code;  // coded coefficients (nullptr: dense; two-pass classes only)
     const T* tab;
 };
 
@@ -2069,44 +2071,227 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T
     });
 }
 
-// The fused step of every instance of one fused class: work items (a tile column and a
-// range of kPoolFusedZlen planes of one instance) in grid-stride order, each marched by
-// fused_march, the code of the single-grid fused kernel.  dir = 0 steps (E, H) ->
-// (E2, H2), dir = 1 back: every fused instance enters a chunk with its state in (E, H)
-// and takes an even number of steps in it, so all of them share the direction of a step.
-template <typename T, int VEC>
-__global__ void __launch_bounds__(32 * (kPoolFusedRows + 1), 3) k_step_fused_pool(const PoolTable<T>* __restrict__ tab,
-                                                                               int dir) {
-    __shared__ FusedShared<T, VEC, kPoolFusedRows> sm;
+// The fused step of every instance of one fused class, on plane segments.  A work item
+// is a segment of kSegCells consecutive cells of the plane-local flat index p = i + Nx*j
+// (it may span several rows: a row of these grids is 48-160 cells) and a range of zlen
+// planes of one instance; the CTA marches it through the planes.  For plane k:
+//   1. each thread computes the new H of its own vectors (hpass_eval, the code of every
+//      other H update), stores it to Hout and to the plane buffer hb, and the CTA
+//      recomputes from the old fields the new H of the Nx cells before the segment
+//      (plane-local p0-Nx .. p0-1; below p = 0 these are flat-index cells of plane k-1,
+//      exactly the -y neighbours the reference's curl couples);
+//   2. after one barrier each thread updates E of its own vectors from hb (the -x and
+//      -y neighbours) and its registers (its own new H, and the new H_x, H_y of the same
+//      cells one plane below, kept from the previous plane).
+// The plane buffer alternates with the plane parity, so one barrier per plane suffices.
+// A range starting at k0 > 0 first computes the new H of plane k0-1 of its own cells
+// (not stored: the range below owns it).  Per cell the step moves E and H once each way
+// and a 2-byte coefficient code (coded contexts only); re-reads of neighbours hit L1/L2.
+// dir = 0 steps (E, H) -> (E2, H2), dir = 1 back: every fused instance enters a chunk
+// with its state in (E, H) and takes an even number of steps in it, so all of them share
+// the direction of a step.
+template <int VEC>
+__host__ __device__ constexpr int seg_reps() {
+    return kSegCells / (kSegTpb * VEC);
+}
+
+// The instance descriptor lives in shared memory.  Its fields are loop-invariant, and
+// the compiler would keep all of them (grid, metric and beam arguments) in registers for
+// the whole march; reading the descriptor through an index it cannot see through, once
+// per phase, makes it reload them from shared memory instead.
+template <typename T>
+__device__ __forceinline__ const PoolInst<T>& seg_desc(const PoolInst<T>* dsh) {
+    int o = 0;
+    asm volatile("" : "+r"(o));
+    return dsh[o];
+}
+
+// (i, j) of the VEC cells of segment vector v (plane-local p = p0 + v*VEC); false past
+// the plane (Nx % VEC == 0: a vector lies in one row)
+__device__ __forceinline__ bool seg_cell(const Geom& g, long long p0, int v, int vec, int& i0, int& j) {
+    const long long p = p0 + (long long)v * vec;
+    if (p >= g.sz) return false;
+    const unsigned q = fdiv((unsigned)p, g.fx);
+    j = (int)q;
+    i0 = (int)((unsigned)p - q * (unsigned)g.nx);
+    return true;
+}
+
+template <typename T, int VEC, int MODE>
+__device__ __forceinline__ void seg_march(const PoolInst<T>* dsh, const T* __restrict__ Ein, const T* __restrict__ Hin,
+                                          T* __restrict__ Eout, T* __restrict__ Hout, long long p0, int k0, int k1,
+                                          T (*hb)[3][kSegMaxNx + kSegCells]) {
+    constexpr int R = seg_reps<VEC>();
+    // the new H_x, H_y of the own cells one plane below
+    T px[R][VEC], py[R][VEC];
+    {
+        const PoolInst<T>& d = seg_desc(dsh);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            zero_v<T, VEC>(px[r]);
+            zero_v<T, VEC>(py[r]);
+            int i0, j;
+            const int v = threadIdx.x + r * kSegTpb;
+            if (k0 > 0 && seg_cell(d.g, p0, v, VEC, i0, j)) {
+                T hz[VEC];
+                const long long n = p0 + (long long)v * VEC + d.g.sz * (k0 - 1);
+                hpass_eval<T, VEC, true>(Ein, Hin, nullptr, d.g, d.mt, n, i0, j, k0 - 1, px[r], py[r], hz, d.code,
+                                         d.tab);
+            }
+        }
+    }
+    for (int k = k0; k < k1; ++k) {
+        T(*b)[kSegMaxNx + kSegCells] = hb[k & 1];
+        T hx[R][VEC], hy[R][VEC], hz[R][VEC];
+        unsigned cd[R][VEC];
+        {
+            const PoolInst<T>& d = seg_desc(dsh);
+            const Geom& g = d.g;
+            const int nx = g.nx;
+            // the Nx cells before the segment, from the old fields (flat index: below p = 0
+            // they wrap into plane k-1; before cell 0 of the grid they are zero); first, so
+            // that no own value is held meanwhile
+            for (int hv = threadIdx.x; hv < nx / VEC; hv += kSegTpb) {
+                const long long m = p0 - nx + (long long)hv * VEC + g.sz * k;
+                T ax[VEC], ay[VEC], az[VEC];
+                if (m >= 0) {
+                    int mi, mj, mk;
+                    cell_of(m, g, mi, mj, mk);
+                    hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, d.mt, m, mi, mj, mk, ax, ay, az, d.code, d.tab);
+                } else {
+                    zero_v<T, VEC>(ax);
+                    zero_v<T, VEC>(ay);
+                    zero_v<T, VEC>(az);
+                }
+                st_v<T, VEC>(&b[0][hv * VEC], ax);
+                st_v<T, VEC>(&b[1][hv * VEC], ay);
+                st_v<T, VEC>(&b[2][hv * VEC], az);
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int v = threadIdx.x + r * kSegTpb;
+                int i0, j;
+                if (!seg_cell(g, p0, v, VEC, i0, j)) continue;
+                const long long n = p0 + (long long)v * VEC + g.sz * k;
+                if constexpr (FIT_FUSED_PREFETCH > 0) {
+                    constexpr int PF = FIT_FUSED_PREFETCH;
+                    if (k + PF + 1 < g.nz) {
+                        prefetch_l2(Ein + n + (PF + 1) * g.sz);
+                        prefetch_l2(Ein + g.N + n + (PF + 1) * g.sz);
+                    }
+                    if (k + PF < g.nz) {
+                        const long long m = n + PF * g.sz;
+                        prefetch_l2(Ein + 2 * g.N + m);
+                        prefetch_l2(Hin + m);
+                        prefetch_l2(Hin + g.N + m);
+                        prefetch_l2(Hin + 2 * g.N + m);
+                        prefetch_l2(d.code + m);
+                    }
+                }
+                ld_codes<VEC>(cd[r], d.code + n);
+                hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, d.mt, n, i0, j, k, hx[r], hy[r], hz[r], d.code, d.tab,
+                                         cd[r]);
+                st_v<T, VEC>(Hout + n, hx[r]);
+                st_v<T, VEC>(Hout + g.N + n, hy[r]);
+                st_v<T, VEC>(Hout + 2 * g.N + n, hz[r]);
+                st_v<T, VEC>(&b[0][nx + v * VEC], hx[r]);
+                st_v<T, VEC>(&b[1][nx + v * VEC], hy[r]);
+                st_v<T, VEC>(&b[2][nx + v * VEC], hz[r]);
+            }
+        }
+        __syncthreads();
+        {
+            const PoolInst<T>& d = seg_desc(dsh);
+            const Geom& g = d.g;
+            const int nx = g.nx;
+            StepArgs st{};
+            st.d_step = d.d_step;
+            st.vt_table = d.vt_table;
+            st.vt_len = d.vt_len;
+            const PlaneArgs pl{};
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int v = threadIdx.x + r * kSegTpb;
+                int i0, j;
+                if (!seg_cell(g, p0, v, VEC, i0, j)) continue;
+                const long long n = p0 + (long long)v * VEC + g.sz * k;
+                T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
+                ld_v<T, VEC>(hxy, &b[0][v * VEC]);  // n - Nx
+                ld_v<T, VEC>(hzy, &b[2][v * VEC]);
+                const T hyx = b[1][nx + v * VEC - 1];  // n - 1
+                const T hzx = b[2][nx + v * VEC - 1];
+                if (k > 0) {
+#pragma unroll
+                    for (int e = 0; e < VEC; ++e) {
+                        hxz[e] = px[r][e];
+                        hyz[e] = py[r][e];
+                    }
+                } else {
+                    zero_v<T, VEC>(hxz);
+                    zero_v<T, VEC>(hyz);
+                }
+                T cur[3][VEC];
+                epass_curl<T, VEC>(hx[r], hy[r], hz[r], hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, d.mt);
+                T kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
+                tab_get_v<T, VEC>(d.tab, cd[r], 1, kx, ky, kz);
+                if constexpr (MODE == 1) {
+                    tab_get_v<T, VEC>(d.tab, cd[r], 2, lx, ly, lz);
+                } else {
+                    zero_v<T, VEC>(lx);
+                    zero_v<T, VEC>(ly);
+                    zero_v<T, VEC>(lz);
+                }
+                T ex[VEC], ey[VEC], ez[VEC];
+                ldg_v<T, VEC>(ex, Ein + n);
+                ldg_v<T, VEC>(ey, Ein + g.N + n);
+                ldg_v<T, VEC>(ez, Ein + 2 * g.N + n);
+                epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, d.J, n, i0, j, k, d.use_cond, g,
+                                           d.beam, pl, st);
+                st_v<T, VEC>(Eout + n, ex);
+                st_v<T, VEC>(Eout + g.N + n, ey);
+                st_v<T, VEC>(Eout + 2 * g.N + n, ez);
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) {
+                    px[r][e] = hx[r][e];
+                    py[r][e] = hy[r][e];
+                }
+            }
+        }
+    }
+}
+
+// MINB: CTAs per SM the register budget is sized for (the launch bound).
+template <typename T, int VEC, int MINB>
+__global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable<T>* __restrict__ tab, int dir) {
+    __shared__ __align__(16) T hb[2][3][kSegMaxNx + kSegCells];
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
     const int ninst = tab->ninst;
     const long long c0 = tab->cls_t0[pool_fused_class(VEC)], c1 = tab->cls_t0[pool_fused_class(VEC) + 1];
+    long long lo_w = 0, hi_w = -1;  // work items of the cached descriptor
+    bool run = false;
     for (long long w = c0 + blockIdx.x; w < c1; w += gridDim.x) {
-        __syncthreads();  // the previous work item no longer reads sm or si
-        pool_fetch<T>(tab, ninst, w, &si, &sn);
-        __syncthreads();
-        if (sn >= si.n_end) continue;
-        const long long local = w - si.tile0;
-        const long long per_z = (long long)si.tiles_x * si.tiles_y;
-        const int bz = (int)(local / per_z);
-        const int rem = (int)(local - bz * per_z);
-        const int by = rem / si.tiles_x, bx = rem - by * si.tiles_x;
-        const int k0 = bz * kPoolFusedZlen, k1 = min(si.g.nz, k0 + kPoolFusedZlen);
+        __syncthreads();  // the previous work item no longer reads hb or si
+        if (w >= hi_w) {
+            pool_fetch<T>(tab, ninst, w, &si, &sn);
+            __syncthreads();
+            lo_w = si.tile0;
+            hi_w = si.tile0 + si.ntile;
+            run = sn < si.n_end;
+        }
+        if (!run) continue;
+        const long long local = w - lo_w;
+        const int zr = (int)(local / si.nseg);
+        const long long p0 = (local - (long long)zr * si.nseg) * kSegCells;
+        const int k0 = zr * si.zlen, k1 = min(si.g.nz, k0 + si.zlen);
         const T* Ein = dir ? si.E2 : si.E;
         const T* Hin = dir ? si.H2 : si.H;
         T* Eout = dir ? si.E : si.E2;
         T* Hout = dir ? si.H : si.H2;
-        StepArgs st{};
-        st.d_step = si.d_step;
-        st.vt_table = si.vt_table;
-        st.vt_len = si.vt_len;
         if (si.mode == 1)
-            fused_march<T, VEC, kPoolFusedRows, 1>(Ein, Hin, Eout, Hout, si.ch, si.ce, si.cl, si.J, si.use_cond, si.g,
-                                                   si.mt, si.beam, st, bx, by, k0, k1, sm);
+            seg_march<T, VEC, 1>(&si, Ein, Hin, Eout, Hout, p0, k0, k1, hb);
         else
-            fused_march<T, VEC, kPoolFusedRows, 0>(Ein, Hin, Eout, Hout, si.ch, si.ce, si.cl, si.J, si.use_cond, si.g,
-                                                   si.mt, si.beam, st, bx, by, k0, k1, sm);
+            seg_march<T, VEC, 0>(&si, Ein, Hin, Eout, Hout, p0, k0, k1, hb);
     }
 }
 

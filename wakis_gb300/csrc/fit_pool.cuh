@@ -27,7 +27,6 @@ struct PoolSlot {
     long long nsteps = 0;
     long long sched = 0;  // steps enqueued so far
     PoolInst<float> row{};
-    long long ntiles = 0;
     cudaEvent_t ready = nullptr;  // end of the caller's work on the context before submit
     bool joined = false;          // the pool stream has waited on `ready`
     double t_submit = 0.0, t_start = -1.0;
@@ -52,7 +51,8 @@ struct FitPool {
     int ctas_per_sm = 0;
     int minb[3]{3, 3, 4};          // kernel variant (CTAs per SM of its register budget) per class
     int grid_h[3]{}, grid_e[3]{};  // persistent CTAs of the pass kernels per vector class
-    int grid_f[2]{};               // persistent CTAs of the fused kernels (4-, 2-wide vectors)
+    int fminb[3]{3, 3, 3};         // fused kernel variant (CTAs per SM) per vector width 4, 2, 1
+    int grid_f[3]{};               // persistent CTAs of the fused kernels (4-, 2-, 1-wide vectors)
     int gen = 0;                   // bumped by fit_pool_tune: captured graphs of older variants are stale
     cudaStream_t ps = nullptr;     // every chunk runs here
     cudaEvent_t ev[2]{};
@@ -70,7 +70,7 @@ struct FitPool {
     bool stop = false;
     int status = FIT_OK;
     std::string err;
-    long long chunks = 0, cell_updates = 0;
+    long long chunks = 0, cell_updates = 0, fused_cell_updates = 0;
     int max_active = 0;
     double busy_ms = 0.0;
     std::chrono::steady_clock::time_point t0;
@@ -145,12 +145,29 @@ void retire_cancelled(FitPool* p, double t) {
     if (any) p->cv_done.notify_all();
 }
 
+// planes per work item of the fused members of a chunk: about kSegWaves work items per
+// CTA of the persistent fused grid, so the last wave of a step is a small part of it,
+// within [kSegZlenMin, kSegZlenMax] (a range start recomputes one plane of H)
+constexpr int kSegWaves = 4;
+constexpr int kSegZlenMin = 8;
+constexpr int kSegZlenMax = 64;
+
+int seg_zlen(const FitPool* p, const std::vector<PoolSlot*>& members) {
+    long long units = 0;  // segment-planes of the fused members
+    for (const PoolSlot* s : members)
+        if (s->row.fused) units += s->row.nseg * s->c->g.nz;
+    const long long grid = std::max({p->grid_f[0], p->grid_f[1], p->grid_f[2], 1});
+    const long long z = units / (kSegWaves * grid);
+    return (int)std::min<long long>(kSegZlenMax, std::max<long long>(kSegZlenMin, z));
+}
+
 // fills pinned table `b` with the members that still have steps to enqueue, ordered by
 // vector class; returns the mask of the classes present
 int stage_table(FitPool* p, int b, const std::vector<PoolSlot*>& members) {
     PoolTable<float>* t = p->h_tab[b];
     long long tile = 0;
     int n = 0, mask = 0;
+    const int zlen = seg_zlen(p, members);
     for (int cls = 0; cls < kPoolClasses; ++cls) {
         t->cls_t0[cls] = tile;
         for (PoolSlot* s : members) {
@@ -158,14 +175,26 @@ int stage_table(FitPool* p, int b, const std::vector<PoolSlot*>& members) {
             if (sc != cls) continue;
             PoolInst<float>& r = t->inst[n++];
             r = s->row;
+            if (r.fused) {
+                r.zlen = zlen;
+                r.ntile = r.nseg * ((r.g.nz + zlen - 1) / zlen);
+            }
             r.tile0 = tile;
-            tile += s->ntiles;
+            tile += r.ntile;
             mask |= 1 << cls;
         }
     }
     t->cls_t0[kPoolClasses] = tile;
     t->ninst = n;
     return mask;
+}
+
+// the pooled fused step serves coded FP32 contexts with the fused step enabled (second
+// field buffers), the elided J, no plane source or ABC update, and Nx <= kSegMaxNx; any
+// Nx % vec == 0 vector width (odd Nx: single cells)
+bool pool_fused_ok(const FitCtx* c, int mode) {
+    return c->fused && c->E2 && c->H2 && mode != 2 && !c->plane.active && !c->abc_axes && c->d_code && c->d_tab &&
+           c->g.nx <= kSegMaxNx;
 }
 
 // compiled variants: launch bound (CTAs per SM) choices per vector class
@@ -198,8 +227,28 @@ cudaError_t pool_grids(int nsm, int cls, int minb, int ctas_per_sm, int* gh, int
 }
 
 struct PoolTune {
-    int minb[3], grid_h[3], grid_e[3], grid_f[2], gen;
+    int minb[3], grid_h[3], grid_e[3], fminb[3], grid_f[3], gen;
 };
+
+// the pooled fused kernel of vector width vec, compiled with the register budgets of 2
+// and 3 CTAs per SM (m)
+bool pool_fminb_ok(int m) { return m == 2 || m == 3; }
+const void* pool_seg_func(int vec, int m) {
+    if (vec == 4)
+        return m == 2 ? (const void*)k_step_seg_pool<float, 4, 2> : (const void*)k_step_seg_pool<float, 4, 3>;
+    if (vec == 2)
+        return m == 2 ? (const void*)k_step_seg_pool<float, 2, 2> : (const void*)k_step_seg_pool<float, 2, 3>;
+    return m == 2 ? (const void*)k_step_seg_pool<float, 1, 2> : (const void*)k_step_seg_pool<float, 1, 3>;
+}
+
+// persistent CTAs of the fused kernel of vector width vec with variant m
+cudaError_t pool_grid_f(int nsm, int vec, int m, int ctas_per_sm, int* grid) {
+    int of = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&of, pool_seg_func(vec, m), kSegTpb, 0);
+    of = std::max(of, 1);
+    *grid = nsm * (ctas_per_sm ? std::min(ctas_per_sm, of) : of);
+    return e;
+}
 
 // kernel entry of class cls's pass with variant m
 const void* pool_pass_func(int cls, int m, bool e_pass) {
@@ -256,11 +305,9 @@ cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraph
                     e = add_node(gr, &prev, pool_pass_func(cls, t.minb[cls], pass == 1),
                                  pass == 1 ? t.grid_e[cls] : t.grid_h[cls], dim3(kPoolTpb), pass_args);
         void* fused_args[2] = {&tab, &dir};
-        const dim3 fused_block(32, kPoolFusedRows + 1);  // lanes along x, one warp per row + the halo warp
-        if (e == cudaSuccess && (mask & (1 << 3)))
-            e = add_node(gr, &prev, (const void*)k_step_fused_pool<float, 4>, t.grid_f[0], fused_block, fused_args);
-        if (e == cudaSuccess && (mask & (1 << 4)))
-            e = add_node(gr, &prev, (const void*)k_step_fused_pool<float, 2>, t.grid_f[1], fused_block, fused_args);
+        for (int f = 0; f < 3 && e == cudaSuccess; ++f)
+            if (mask & (1 << (3 + f)))
+                e = add_node(gr, &prev, pool_seg_func(4 >> f, t.fminb[f]), t.grid_f[f], dim3(kSegTpb), fused_args);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b][mask], gr, 0);
     if (gr) cudaGraphDestroy(gr);
@@ -313,8 +360,10 @@ void pool_main(FitPool* p) {
                     tune.grid_h[c] = p->grid_h[c];
                     tune.grid_e[c] = p->grid_e[c];
                 }
-                tune.grid_f[0] = p->grid_f[0];
-                tune.grid_f[1] = p->grid_f[1];
+                for (int f = 0; f < 3; ++f) {
+                    tune.fminb[f] = p->fminb[f];
+                    tune.grid_f[f] = p->grid_f[f];
+                }
                 tune.gen = p->gen;
             }
         }
@@ -342,7 +391,7 @@ void pool_main(FitPool* p) {
             f.buf = b;
             f.t_launch = p->now();
             if (busy_since < 0) busy_since = f.t_launch;
-            long long cells = 0;
+            long long cells = 0, fcells = 0;
             {
                 std::lock_guard<std::mutex> lk(p->mu);  // inflight is read by retire_cancelled
                 for (PoolSlot* s : members) {
@@ -351,6 +400,7 @@ void pool_main(FitPool* p) {
                     s->sched += take;
                     s->inflight++;
                     cells += take * s->c->g.N;
+                    if (s->row.fused) fcells += take * s->c->g.N;
                     if (s->sched >= s->nsteps) f.finishing.push_back(s);
                 }
             }
@@ -359,6 +409,7 @@ void pool_main(FitPool* p) {
                 std::lock_guard<std::mutex> lk(p->mu);
                 p->chunks++;
                 p->cell_updates += cells;
+                p->fused_cell_updates += fcells;
                 p->max_active = std::max(p->max_active, n);
             }
             fl.push_back(std::move(f));
@@ -436,13 +487,7 @@ int fit_pool_create(int32_t device, int64_t budget_bytes, int32_t chunk_steps, i
     p->ctas_per_sm = ctas_per_sm;
     for (int c = 0; c < 3 && e == cudaSuccess; ++c)
         e = pool_grids(p->nsm, c, p->minb[c], ctas_per_sm, &p->grid_h[c], &p->grid_e[c]);
-    int of4 = 0, of2 = 0;
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&of4, k_step_fused_pool<float, 4>, 32 * (kPoolFusedRows + 1), 0);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&of2, k_step_fused_pool<float, 2>, 32 * (kPoolFusedRows + 1), 0);
-    p->grid_f[0] = p->nsm * std::max(of4, 1);
-    p->grid_f[1] = p->nsm * std::max(of2, 1);
+    for (int f = 0; f < 3 && e == cudaSuccess; ++f) e = pool_grid_f(p->nsm, 4 >> f, p->fminb[f], ctas_per_sm, &p->grid_f[f]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->ps, cudaStreamNonBlocking);
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         e = cudaEventCreateWithFlags(&p->ev[b], cudaEventDisableTiming | cudaEventBlockingSync);
@@ -532,11 +577,11 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     static thread_local long long host_n0;
     host_n0 = n0;
     CK(cudaMemcpyAsync(c->d_step, &host_n0, sizeof(long long), cudaMemcpyHostToDevice, c->own));
-    // a context with the fused step enabled is stepped by the pooled fused kernel; it
-    // takes its steps in pairs (ending in E, H), so an odd count takes its first step
-    // here with the two-pass kernels
+    // a coded context with the fused step enabled is stepped by the pooled fused kernel
+    // (when the chunk length is even); it takes its steps in pairs (ending in E, H), so an
+    // odd count takes its first step here with the two-pass kernels
     const int mode = c->use_cond ? 1 : 0;
-    const bool fused = fused_ok(c, mode);
+    const bool fused = pool_fused_ok(c, mode) && p->chunk % 2 == 0;
     long long pooled = nsteps;
     if (fused && (nsteps % 2)) {
         launch_step(c, 0, mode, true);
@@ -564,10 +609,10 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     r.ce = static_cast<const float*>(c->ce);
     r.cl = static_cast<const float*>(c->cl);
     r.J = static_cast<float*>(c->J);
-    // the two-pass classes read the context's coefficient codes when it has them (the
-    // pooled fused class keeps the dense arrays)
-    r.code = fused ? nullptr : c->d_code;
-    r.tab = fused ? nullptr : static_cast<const float*>(c->d_tab);
+    // every class reads the context's coefficient codes when it has them (the fused
+    // class only takes coded contexts)
+    r.code = c->d_code;
+    r.tab = static_cast<const float*>(c->d_tab);
     r.beam = c->beam;
     r.tap = c->tap;
     r.d_step = c->d_step;
@@ -583,11 +628,10 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
         r.fused = 1;
         r.E2 = static_cast<float*>(c->E2);
         r.H2 = static_cast<float*>(c->H2);
-        r.tiles_x = (c->g.nx + 32 * r.vec - 1) / (32 * r.vec);
-        r.tiles_y = (c->g.ny + kPoolFusedRows - 1) / kPoolFusedRows;
-        r.ntile = (long long)r.tiles_x * r.tiles_y * ((c->g.nz + kPoolFusedZlen - 1) / kPoolFusedZlen);
+        r.nseg = (c->g.sz + kSegCells - 1) / kSegCells;
+        r.zlen = kSegZlenMax;  // set per chunk by stage_table
+        r.ntile = r.nseg * ((c->g.nz + r.zlen - 1) / r.zlen);
     }
-    s->ntiles = r.ntile;
     c->in_pool = true;
     {
         std::lock_guard<std::mutex> lk(p->mu);
@@ -654,6 +698,25 @@ int fit_pool_tune(FitPool* p, int32_t vec, int32_t ctas_per_sm) {
     return FIT_OK;
 }
 
+int fit_pool_tune_fused(FitPool* p, int32_t vec, int32_t ctas_per_sm) {
+    if (!p || (vec != 4 && vec != 2 && vec != 1)) return FIT_ERR_ARG;
+    if (!pool_fminb_ok(ctas_per_sm)) {
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->err = "no compiled fused pool kernel variant for that CTAs per SM (2 or 3)";
+        return FIT_ERR_ARG;
+    }
+    const int f = vec == 4 ? 0 : (vec == 2 ? 1 : 2);
+    int gf = 0;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e == cudaSuccess) e = pool_grid_f(p->nsm, vec, ctas_per_sm, p->ctas_per_sm, &gf);
+    if (e != cudaSuccess) return pool_fail(p, FIT_ERR_CUDA, "fit_pool_tune_fused: %s", cudaGetErrorString(e));
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->fminb[f] = ctas_per_sm;
+    p->grid_f[f] = gf;
+    p->gen++;
+    return FIT_OK;
+}
+
 int fit_pool_stats(FitPool* p, FitPoolStats* out) {
     if (!p || !out) return FIT_ERR_ARG;
     std::lock_guard<std::mutex> lk(p->mu);
@@ -671,6 +734,11 @@ int fit_pool_stats(FitPool* p, FitPoolStats* out) {
     }
     s.chunk_steps = p->chunk;
     s.busy_ms = p->busy_ms;
+    s.fused_cell_updates = p->fused_cell_updates;
+    for (int f = 0; f < 3; ++f) {
+        s.fused_variant[f] = p->fminb[f];
+        s.fused_grid[f] = p->grid_f[f];
+    }
     *out = s;
     return FIT_OK;
 }

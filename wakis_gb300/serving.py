@@ -157,7 +157,8 @@ class ServedSolve:
         self.grid, self.wake, self.solver = build(req, dtype, device, results_folder)
         s = self.solver
         # 'direct': the pool's two-pass kernels; 'fused' (or 'auto' with Nx even): the
-        # pool's fused kernel, which also holds the second E, H buffers
+        # pool's fused step on plane segments (coded coefficients, Nx <= 256; any other
+        # grid takes the two-pass kernels), which also holds the second E, H buffers
         s.kernels = kernels
         self.beam, self.Nt = s._wake_prepare(self.wake, req.wakelength, "both")
         self.vt = s._wake_device_setup(self.beam, self.Nt)
@@ -198,6 +199,7 @@ def solve_alone(req, dtype=np.float32, device=0, dt=None, kernels="auto"):
 
 
 POOL_VARIANTS = {4: (2, 3), 2: (2, 3), 1: (3, 4)}
+POOL_FUSED_VARIANTS = (2, 3)  # CTAs per SM of the pooled fused kernel's compiled register budgets
 
 
 def run_resident(pool, reqs, kernels="direct"):
@@ -235,20 +237,23 @@ def calibration_requests(seed=11, per_class=4, wakelength=0.1):
     return out
 
 
-def autotune(pool, calib=None, repeats=1):
-    """Per vector-width class, times every compiled pass-kernel variant of the pool on
-    calibration grids (all resident at once, pool time only) and keeps the fastest.
+def autotune(pool, calib=None, repeats=1, kernels="direct"):
+    """Per vector-width class, times every compiled variant of the pool's kernels on
+    calibration grids (all resident at once, pool time only) and keeps the fastest:
+    the two-pass kernels with kernels='direct', the fused step with kernels='fused'.
     Returns {vec: {"choice": ctas_per_sm, "rates": {variant: cell-updates/s}}}."""
     import torch
     calib = calib or calibration_requests()
+    fused = kernels == "fused"
+    select = pool.tune_fused if fused else pool.tune
     out = {}
     for vec, reqs in calib.items():
         rates = {}
-        for minb in POOL_VARIANTS[vec]:
-            pool.tune(vec, minb)
+        for minb in (POOL_FUSED_VARIANTS if fused else POOL_VARIANTS[vec]):
+            select(vec, minb)
             best = 0.0
             for _ in range(repeats):
-                cu, busy, jobs = run_resident(pool, reqs, kernels="direct")
+                cu, busy, jobs = run_resident(pool, reqs, kernels=kernels)
                 for j in jobs:
                     j.close()
                 del jobs
@@ -256,7 +261,7 @@ def autotune(pool, calib=None, repeats=1):
                 best = max(best, cu / busy if busy > 0 else 0.0)
             rates[minb] = best
         choice = max(rates, key=rates.get)
-        pool.tune(vec, choice)
+        select(vec, choice)
         out[vec] = {"choice": choice, "rates": rates}
     return out
 
@@ -324,11 +329,13 @@ class ServingLoop:
     ``trace_path`` every record is also appended to that file as one JSON line."""
 
     def __init__(self, budget_bytes, chunk_steps=64, ctas_per_sm=0, device=0, dtype=np.float32, max_bypass=8,
-                 keep_results=True, variants=None, kernels="direct", trace_path=None):
+                 keep_results=True, variants=None, kernels="direct", trace_path=None, fused_variants=None):
         self.budget = int(budget_bytes)
         self.pool = nat.Pool(budget_bytes, chunk_steps=chunk_steps, ctas_per_sm=ctas_per_sm, device=device)
         for vec, minb in (variants or {}).items():
             self.pool.tune(vec, minb)
+        for vec, minb in (fused_variants or {}).items():
+            self.pool.tune_fused(vec, minb)
         self.device = device
         self.dtype = dtype
         self.kernels = kernels
