@@ -357,6 +357,9 @@ def run_ours(args, rank, world):
                  "traffic": profile_traffic("fused_coded_cfg4_ncu.md" if coded else "fused_cfg4_ncu.md"),
                  "algorithmic_bytes_per_launch": bytes_cell * N, "ms_per_launch": kf[0],
                  "peak_source": f"{src} HBM copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"}
+        fused["traffic_source"] = ("profiles/%s: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
+                                   "the 256x256x512 grid, scaled by the cell count (x8)"
+                                   % ("fused_coded_cfg4_ncu.md" if coded else "fused_cfg4_ncu.md"))
         if coded:
             ach_model = BYTES_STEP_MODEL * N / (kf[0] / 1e3) / 1e9
             fused["coefficient_codes"] = s.coefficient_code_count
@@ -381,6 +384,32 @@ def run_ours(args, rank, world):
                              "note": "84 B/cell-update = fused-step algorithmic bytes; the two-pass step moves "
                                      "108 B/cell"},
            "gpu_launches": int(launches)}
+    out["roofline"]["traffic_source"] = ("profiles/%s: ncu dram bytes of one launch on the 256x256x512 grid, "
+                                         "scaled by the cell count (x8)"
+                                         % ("epass_coded_cfg4_ncu.md" if coded else "epass_cfg4_ncu.md"))
+    if fused is not None and coded and not args.no_dense_roofline:
+        # the dense fused step on the same grid (84 B per cell-update: ch, ce, cl read per
+        # cell), the step a grid with more than 65535 distinct coefficient triples runs
+        s.coefficient_codes = False
+        s._ensure_codes()
+        s._ctx.call("fit_set_fused_staging", 0, 0)
+        kd = np.zeros(2)
+        dense_ms = {}
+        for shape in ((4, 4, 64, 3), (4, 4, 64, 4), (4, 8, 64, 2), (4, 4, 32, 3)):
+            s._ctx.call("fit_set_fused_shape", *shape)
+            s._ctx.call("fit_time_fused", 10, nat.dptr(kd))
+            dense_ms[shape] = float(kd[0])
+        shape = min(dense_ms, key=dense_ms.get)
+        ach_d = BYTES_STEP_MODEL * N / (dense_ms[shape] / 1e3) / 1e9
+        out["roofline_dense"] = {"bound": "hbm", "kernel": "k_step_fused (whole step, lossy, FP32, dense coefficients)",
+                                 "achieved": ach_d, "peak": peak, "unit": "GB/s", "frac": ach_d / peak,
+                                 "algorithmic_bytes_per_launch": BYTES_STEP_MODEL * N, "ms_per_launch": dense_ms[shape],
+                                 "shape": {"vec": shape[0], "rows": shape[1], "zseg": shape[2], "ctas": shape[3]},
+                                 "ms_by_shape": {"v%dr%dz%dc%d" % k: t for k, t in dense_ms.items()},
+                                 "traffic": profile_traffic("fused_cfg4_ncu.md"),
+                                 "traffic_source": "profiles/fused_cfg4_ncu.md (ncu, 256x256x512 grid, scaled x8)",
+                                 "note": "the fused step of a grid whose coefficients do not compress (more than "
+                                         "65535 distinct triples, e.g. graded spacing): 84 B per cell-update"}
     if fused is not None:
         out["roofline_two_pass_e"] = out["roofline"]
         out["roofline"] = fused
@@ -405,12 +434,117 @@ def run_ours(args, rank, world):
     torch.cuda.empty_cache()
     if not args.no_e2e:
         out["e2e"] = e2e(wg, torch, dev, P, args.variant)
+    if rank == 0 and world == 1 and not args.no_serve:
+        out["serving"] = serving_summary(args, peak)
     if rank == 0 and not args.no_cpu:
         rate, sample, cores = cpu_sample_parallel()
         out["cpu_baseline"] = {"value": rate, "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
                                "sample": sample}
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def serving_summary(args, peak):
+    """The served path, measured in the default run on one GPU (BASELINE metric, second
+    half): the 64-request cavity sweep (cube 20-60 mm, n 48-160, default_rng(seed=3)),
+    arriving as a Poisson stream at which the 4 GB memory budget binds, served in FP32 by
+    the pool with continuous batching (two-pass kernel variants chosen by the autotuner on
+    calibration grids); the pool's throughput with every request resident, over the first
+    0.1 m of wake (a per-step rate, which the wake length does not change), against the
+    measured HBM bandwidth; and the plain FP64 path one request at a time on a seeded
+    subsample, which gives the FP64 solves/h and each subsampled request's WP / Z error of
+    the served FP32 result (the FP64 runs take the FP32 time step)."""
+    import gc
+    import torch
+    from wakis_gb300 import serving as S
+    from wakis_gb300 import _native as nat
+
+    def free():
+        gc.collect()
+        torch.cuda.empty_cache()
+
+    t_all = time.perf_counter()
+    budget = int(args.serve_budget_gb * 1e9)
+    base = S.config3_requests(args.serve_count, seed=3)
+    rate = S.poisson_rate_for(base, budget, args.serve_ref_rate * 1e9, load=args.serve_load)
+    reqs = S.config3_requests(args.serve_count, seed=3, rate_hz=rate)
+    out = {"workload": f"{len(reqs)} cavity wake solves (cube 20-60 mm, pipe 3-8 mm, n 48-160, z 2n, sigma_z 5-15 mm, "
+                       f"PEC or sigma 1e3-1e6 S/m, wake 1 m), default_rng(seed=3)",
+           "budget_bytes": budget, "arrival_rate_hz": rate, "chunk_steps": args.serve_chunk,
+           "arrivals": f"Poisson, {args.serve_load}x the service rate of {args.serve_ref_rate} G cell-updates/s"}
+    warm = [S.CavityRequest(tag=1000 + i, side=20e-3, rp=4e-3, n=16 + 2 * i, sigmaz=6e-3, sigma=1e4 * i,
+                            wakelength=0.05) for i in range(2)]
+    loop = S.ServingLoop(budget, chunk_steps=args.serve_chunk, keep_results=False)
+    loop.run(warm)
+    loop.close()
+    t0 = time.perf_counter()
+    tpool = nat.Pool(32 << 30, chunk_steps=args.serve_chunk)
+    tuned = S.autotune(tpool)
+    tpool.close()
+    free()
+    variants = {vec: r["choice"] for vec, r in tuned.items()}
+    out["autotune"] = {"seconds": time.perf_counter() - t0, "choice": {str(v): m for v, m in variants.items()}}
+    # FP32 served, Poisson arrivals, memory admission
+    loop = S.ServingLoop(budget, chunk_steps=args.serve_chunk, variants=variants)
+    recs, summ = loop.run(reqs)
+    res32 = loop.results
+    loop.close()
+    free()
+    out["solves_per_hour"] = summ["solves_per_hour"]
+    out["tti_p50_s"], out["tti_p99_s"] = summ["tti_p50_s"], summ["tti_p99_s"]
+    out["makespan_s"] = summ["makespan_s"]
+    out["mcell_updates_per_s"] = summ["mcell_updates_per_s"]
+    out["solves"], out["failed"] = summ["solves"], summ["failed"]
+    out["max_resident"] = summ["pool"]["max_active"]
+    # every request resident: the pool's per-step throughput against the bytes its coded
+    # two-pass kernels move (76 B per cell-update: E and H read and written once per pass
+    # and a 2-byte code per pass) and against the 72 / 84 B per cell-update model
+    short = S.config3_requests(args.serve_count, seed=3, wakelength=0.1)
+    pool = nat.Pool(sum(S.footprint_bytes(r) for r in short) + (1 << 30), chunk_steps=args.serve_chunk)
+    for vec, m in variants.items():
+        pool.tune(vec, m)
+    cu, busy, jobs = S.run_resident(pool, short, kernels="direct")
+    st = pool.stats()
+    pool.close()
+    coded = all(j.solver.coefficient_code_count > 0 for j in jobs)
+    moved = sum((76 if j.solver.coefficient_code_count > 0 else (108 if j.req.lossy else 96)) * j.req.cells
+                * (j.Nt - j.first) for j in jobs)
+    model = sum((84 if j.req.lossy else 72) * j.req.cells * (j.Nt - j.first) for j in jobs)
+    for j in jobs:
+        j.close()
+    del jobs
+    free()
+    out["all_resident"] = {"requests": len(short), "wake_m": 0.1, "seconds": busy, "mcell_updates_per_s": cu / busy / 1e6,
+                           "hbm_gbs": moved / busy / 1e9, "hbm_frac": moved / busy / 1e9 / peak,
+                           "hbm_frac_model": model / busy / 1e9 / peak, "coded": coded, "chunks": st["chunks"],
+                           "bytes": "hbm_frac on the 76 B per cell-update the coded two-pass kernels move; "
+                                    "hbm_frac_model on the 72 B (PEC) / 84 B (lossy) model"}
+    # plain FP64 one at a time on a subsample: solves/h and the FP32 results' errors
+    rng = np.random.default_rng(5)
+    sub = sorted(rng.choice(len(reqs), size=min(args.serve_fp64_sample, len(reqs)), replace=False).tolist())
+    res64 = {}
+    t0 = time.perf_counter()
+    for i in sub:
+        r = reqs[i]
+        res64[r.tag] = S.solve_alone(r, np.float64, dt=S.cfl_dt(r, np.float32), kernels="auto")
+        torch.cuda.synchronize()
+        free()
+    sec64 = time.perf_counter() - t0
+    frac_work = sum(reqs[i].cells * S._steps_estimate(reqs[i]) for i in sub) / sum(
+        r.cells * S._steps_estimate(r) for r in reqs)
+    fp64_sph = len(reqs) * 3600.0 * frac_work / sec64  # the whole sweep at the subsample's rate
+    wp = {t: _rel(res32[t]["WP"], res64[t]["WP"]) for t in res64 if t in res32}
+    zz = {t: _rel(res32[t]["Z"], res64[t]["Z"]) for t in res64 if t in res32}
+    out["plain_fp64_one_at_a_time"] = {
+        "sample": f"{len(sub)} of {len(reqs)} requests (default_rng(5)), run back to back; solves/h scaled by their "
+                  f"share of the sweep's cell-updates ({frac_work:.3f})",
+        "seconds": sec64, "solves_per_hour": fp64_sph}
+    out["speedup_solves_per_hour_vs_fp64"] = summ["solves_per_hour"] / fp64_sph
+    out["accuracy_vs_fp64"] = {"WP_rel_l2_max": max(wp.values()), "WP_rel_l2_median": float(np.median(list(wp.values()))),
+                               "Z_rel_l2_max": max(zz.values()), "requests": len(wp),
+                               "requests_above_1e-4": int(sum(e > 1e-4 for e in wp.values()))}
+    out["seconds"] = time.perf_counter() - t_all
+    return out
 
 
 def e2e(wg, torch, dev, P, kernels="direct"):
@@ -708,6 +842,10 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-no-fp64", action="store_true")
     ap.add_argument("--serve-no-saturated", action="store_true")
+    ap.add_argument("--serve-fp64-sample", type=int, default=8,
+                    help="requests of the sweep run through the plain FP64 path in the default line")
+    ap.add_argument("--no-serve", action="store_true", help="default line without the serving block")
+    ap.add_argument("--no-dense-roofline", action="store_true", help="default line without the dense fused step timing")
     ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
                     help="with --fused-shape: 0 loads, 1 or 2 TMA plane rings")
     ap.add_argument("--fused-shape", type=int, nargs=4, default=None, metavar=("VEC", "ROWS", "ZSEG", "CTAS"),

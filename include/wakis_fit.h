@@ -364,8 +364,8 @@ FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
  * The serving layer's autotuner times the variants on the requests' own grids. */
 FIT_API int fit_pool_tune(FitPool *pool, int32_t vec, int32_t ctas_per_sm);
 /* Chooses the variant of the pooled fused step for one vector-width class (vec = 4, 2
- * or 1): ctas_per_sm 2 or 3 (the default) names the register budget it was compiled
- * for.  Applies from the next chunk.  No counterpart in the reference (one solve per
+ * or 1): ctas_per_sm names the register budget it was compiled for (vec 4: 2 or 3, vec
+ * 2: 3 or 4, vec 1: 3 or 4; the defaults are 3, 3 and 4).  Applies from the next chunk.  No counterpart in the reference (one solve per
  * process there); the serving layer's autotuner calls it. */
 FIT_API int fit_pool_tune_fused(FitPool *pool, int32_t vec, int32_t ctas_per_sm);
 

@@ -221,19 +221,20 @@ def test_fused_pool_equals_two_pass_wakesolve_bitwise(alone):
         j.close()
 
 
-@pytest.mark.parametrize("minb", [2, 3])
-def test_fused_pool_multi_segment_planes_bitwise(minb):
-    """Planes of several segments (Nx*Ny = 2304 .. 2500 cells for 1024-cell segments, so
-    the cells before a segment are the previous segment's, in the same plane), both
-    compiled register budgets, a chunk length that ends solves inside a chunk: bit for bit
-    the two-pass wakesolve."""
+@pytest.mark.parametrize("choice", [0, 1])
+def test_fused_pool_multi_segment_planes_bitwise(choice):
+    """Planes of several segments (Nx*Ny = 2304 .. 2500 cells, segments of 1024 - Nx
+    cells, so the cells before a segment are the previous segment's, in the same plane),
+    both compiled register budgets, a chunk length that ends solves inside a chunk: bit for
+    bit the two-pass wakesolve."""
     reqs = [S.CavityRequest(tag=10, side=30e-3, rp=5e-3, n=48, sigmaz=8e-3, sigma=0.0, wakelength=0.02),
             S.CavityRequest(tag=11, side=32e-3, rp=6e-3, n=50, sigmaz=9e-3, sigma=3e4, wakelength=0.02),
             S.CavityRequest(tag=12, side=28e-3, rp=4e-3, n=49, sigmaz=7e-3, sigma=0.0, wakelength=0.02)]
     refs = {r.tag: S.solve_alone(r, np.float32, kernels="direct") for r in reqs}
     jobs = [S.ServedSolve(r, kernels="fused") for r in reqs]
-    stats = _run_pool(jobs, chunk_steps=10, variants={4: minb, 2: minb, 1: minb})
-    assert stats["fused_variant"] == {4: minb, 2: minb, 1: minb}
+    variants = {vec: S.POOL_FUSED_VARIANTS[vec][choice] for vec in (4, 2, 1)}
+    stats = _run_pool(jobs, chunk_steps=10, variants=variants)
+    assert stats["fused_variant"] == variants
     assert stats["fused_cell_updates"] == stats["cell_updates"]
     for j in jobs:
         assert_same(j.finish(), refs[j.req.tag])

@@ -1913,8 +1913,8 @@ constexpr int kPoolTpb = 256;
 // enabled and Nx <= kSegMaxNx)
 constexpr int kPoolClasses = 6;
 constexpr int kSegTpb = 256;    // threads of a fused CTA
-constexpr int kSegCells = 1024; // cells of a plane segment (every vector width)
-constexpr int kSegMaxNx = 256;  // the fused class holds grids with Nx up to this
+constexpr int kSegWin = 1024;   // cells of the H window per plane: a segment and the Nx cells before it
+constexpr int kSegMaxNx = 256;  // the fused class holds grids with Nx up to this (segments of >= 768 cells)
 
 __host__ __device__ constexpr int pool_class(int vec) { return vec == 4 ? 0 : (vec == 2 ? 1 : 2); }
 __host__ __device__ constexpr int pool_fused_class(int vec) { return vec == 4 ? 3 : (vec == 2 ? 4 : 5); }
@@ -1945,7 +1945,7 @@ struct PoolInst {
     int use_cond;
     int fused;        // 1: stepped by k_step_seg_pool
     int zlen;         // fused: planes per work item
-    long long nseg;   // fused: plane segments, ceil(Nx*Ny / kSegCells)
+    long long nseg;   // fused: plane segments, ceil(Nx*Ny / (kSegWin - Nx))
     const unsigned short* code;  // coded coefficients (nullptr: dense; two-pass classes only)
     const T* tab;
 };
@@ -2072,27 +2072,26 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T
 }
 
 // The fused step of every instance of one fused class, on plane segments.  A work item
-// is a segment of kSegCells consecutive cells of the plane-local flat index p = i + Nx*j
-// (it may span several rows: a row of these grids is 48-160 cells) and a range of zlen
-// planes of one instance; the CTA marches it through the planes.  For plane k:
-//   1. each thread computes the new H of its own vectors (hpass_eval, the code of every
-//      other H update), stores it to Hout and to the plane buffer hb, and the CTA
-//      recomputes from the old fields the new H of the Nx cells before the segment
-//      (plane-local p0-Nx .. p0-1; below p = 0 these are flat-index cells of plane k-1,
-//      exactly the -y neighbours the reference's curl couples);
-//   2. after one barrier each thread updates E of its own vectors from hb (the -x and
-//      -y neighbours) and its registers (its own new H, and the new H_x, H_y of the same
-//      cells one plane below, kept from the previous plane).
-// The plane buffer alternates with the plane parity, so one barrier per plane suffices.
-// A range starting at k0 > 0 first computes the new H of plane k0-1 of its own cells
-// (not stored: the range below owns it).  Per cell the step moves E and H once each way
-// and a 2-byte coefficient code (coded contexts only); re-reads of neighbours hit L1/L2.
-// dir = 0 steps (E, H) -> (E2, H2), dir = 1 back: every fused instance enters a chunk
-// with its state in (E, H) and takes an even number of steps in it, so all of them share
-// the direction of a step.
+// is a segment of S = kSegWin - Nx consecutive cells of the plane-local flat index
+// p = i + Nx*j (it spans several rows: a row of these grids is 48-256 cells) and a range
+// of zlen planes of one instance; the CTA marches it through the planes.  Per plane k:
+//   1. the CTA computes the new H (hpass_eval, the code of every other H update) of a
+//      window of kSegWin cells: the segment and the Nx cells before it (plane-local
+//      p0-Nx .. p0-1; below p = 0 these are flat-index cells of plane k-1, the -y
+//      neighbours the reference's curl couples), every thread the same number of
+//      vectors; it stores the window to the plane buffer and the segment to Hout;
+//   2. after one barrier each thread updates E of segment cells from the plane buffers
+//      of planes k (own, -x and -y neighbours) and k-1 (the -z neighbour).
+// Three plane buffers rotate, so one barrier per plane suffices and no value is held in
+// registers across it.  A range starting at k0 > 0 first computes the window of plane
+// k0-1 (not stored: the range below owns it).  Per cell the step moves E and H once each
+// way and a 2-byte coefficient code; the re-reads of neighbours and of the window's
+// first Nx cells hit L1/L2.  dir = 0 steps (E, H) -> (E2, H2), dir = 1 back: every
+// fused instance enters a chunk with its state in (E, H) and takes an even number of
+// steps in it, so all of them share the direction of a step.
 template <int VEC>
 __host__ __device__ constexpr int seg_reps() {
-    return kSegCells / (kSegTpb * VEC);
+    return kSegWin / (kSegTpb * VEC);
 }
 
 // The instance descriptor lives in shared memory.  Its fields are loop-invariant, and
@@ -2106,156 +2105,132 @@ __device__ __forceinline__ const PoolInst<T>& seg_desc(const PoolInst<T>* dsh) {
     return dsh[o];
 }
 
-// (i, j) of the VEC cells of segment vector v (plane-local p = p0 + v*VEC); false past
-// the plane (Nx % VEC == 0: a vector lies in one row)
-__device__ __forceinline__ bool seg_cell(const Geom& g, long long p0, int v, int vec, int& i0, int& j) {
-    const long long p = p0 + (long long)v * vec;
-    if (p >= g.sz) return false;
-    const unsigned q = fdiv((unsigned)p, g.fx);
-    j = (int)q;
-    i0 = (int)((unsigned)p - q * (unsigned)g.nx);
-    return true;
+// New H of the window of plane k into plane buffer hb[k % 3]; the segment's cells also to
+// Hout when store is set.  Window vector u covers plane-local p0 - Nx + u*VEC.
+template <typename T, int VEC>
+__device__ __forceinline__ void seg_hwindow(const PoolInst<T>& d, const T* __restrict__ Ein,
+                                            const T* __restrict__ Hin, T* __restrict__ Hout, long long p0, int k,
+                                            bool store, T (*hb)[3][kSegWin]) {
+    constexpr int R = seg_reps<VEC>();
+    const Geom& g = d.g;
+    T(*b)[kSegWin] = hb[k % 3];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int u = threadIdx.x + r * kSegTpb;
+        const long long p = p0 - g.nx + (long long)u * VEC;
+        if (p >= g.sz) continue;  // past the plane (last segment): never read
+        const long long m = p + g.sz * k;
+        T ax[VEC], ay[VEC], az[VEC];
+        if (m >= 0) {
+            int i0, j, kk;
+            if (p >= 0) {
+                const unsigned q = fdiv((unsigned)p, g.fx);
+                j = (int)q;
+                i0 = (int)((unsigned)p - q * (unsigned)g.nx);
+                kk = k;
+            } else {
+                cell_of(m, g, i0, j, kk);
+            }
+            if constexpr (FIT_FUSED_PREFETCH > 0) {
+                constexpr int PF = FIT_FUSED_PREFETCH;
+                if (store && p >= p0) {  // first-touch data of the segment PF planes ahead
+                    if (k + PF + 1 < g.nz) {
+                        prefetch_l2(Ein + m + (PF + 1) * g.sz);
+                        prefetch_l2(Ein + g.N + m + (PF + 1) * g.sz);
+                    }
+                    if (k + PF < g.nz) {
+                        const long long f = m + PF * g.sz;
+                        prefetch_l2(Ein + 2 * g.N + f);
+                        prefetch_l2(Hin + f);
+                        prefetch_l2(Hin + g.N + f);
+                        prefetch_l2(Hin + 2 * g.N + f);
+                        prefetch_l2(d.code + f);
+                    }
+                }
+            }
+            hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, d.mt, m, i0, j, kk, ax, ay, az, d.code, d.tab);
+            if (store && p >= p0) {
+                st_v<T, VEC>(Hout + m, ax);
+                st_v<T, VEC>(Hout + g.N + m, ay);
+                st_v<T, VEC>(Hout + 2 * g.N + m, az);
+            }
+        } else {
+            zero_v<T, VEC>(ax);
+            zero_v<T, VEC>(ay);
+            zero_v<T, VEC>(az);
+        }
+        st_v<T, VEC>(&b[0][u * VEC], ax);
+        st_v<T, VEC>(&b[1][u * VEC], ay);
+        st_v<T, VEC>(&b[2][u * VEC], az);
+    }
 }
 
 template <typename T, int VEC, int MODE>
 __device__ __forceinline__ void seg_march(const PoolInst<T>* dsh, const T* __restrict__ Ein, const T* __restrict__ Hin,
                                           T* __restrict__ Eout, T* __restrict__ Hout, long long p0, int k0, int k1,
-                                          T (*hb)[3][kSegMaxNx + kSegCells]) {
+                                          T (*hb)[3][kSegWin]) {
     constexpr int R = seg_reps<VEC>();
-    // the new H_x, H_y of the own cells one plane below
-    T px[R][VEC], py[R][VEC];
-    {
+    if (k0 > 0) seg_hwindow<T, VEC>(seg_desc(dsh), Ein, Hin, Hout, p0, k0 - 1, false, hb);
+    for (int k = k0; k < k1; ++k) {
+        seg_hwindow<T, VEC>(seg_desc(dsh), Ein, Hin, Hout, p0, k, true, hb);
+        __syncthreads();
         const PoolInst<T>& d = seg_desc(dsh);
+        const Geom& g = d.g;
+        const int nx = g.nx;
+        T(*b)[kSegWin] = hb[k % 3];
+        T(*bm)[kSegWin] = hb[(k + 2) % 3];  // plane k-1
+        StepArgs st{};
+        st.d_step = d.d_step;
+        st.vt_table = d.vt_table;
+        st.vt_len = d.vt_len;
+        const PlaneArgs pl{};
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            zero_v<T, VEC>(px[r]);
-            zero_v<T, VEC>(py[r]);
-            int i0, j;
-            const int v = threadIdx.x + r * kSegTpb;
-            if (k0 > 0 && seg_cell(d.g, p0, v, VEC, i0, j)) {
-                T hz[VEC];
-                const long long n = p0 + (long long)v * VEC + d.g.sz * (k0 - 1);
-                hpass_eval<T, VEC, true>(Ein, Hin, nullptr, d.g, d.mt, n, i0, j, k0 - 1, px[r], py[r], hz, d.code,
-                                         d.tab);
+            const int v = threadIdx.x + r * kSegTpb;  // segment vector
+            const int x = nx + v * VEC;               // its window column
+            const long long p = p0 + (long long)v * VEC;
+            if (x >= kSegWin || p >= g.sz) continue;
+            const long long n = p + g.sz * k;
+            const unsigned q = fdiv((unsigned)p, g.fx);
+            const int j = (int)q;
+            const int i0 = (int)((unsigned)p - q * (unsigned)nx);
+            T hx[VEC], hy[VEC], hz[VEC], hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
+            ld_v<T, VEC>(hx, &b[0][x]);
+            ld_v<T, VEC>(hy, &b[1][x]);
+            ld_v<T, VEC>(hz, &b[2][x]);
+            ld_v<T, VEC>(hxy, &b[0][x - nx]);  // n - Nx
+            ld_v<T, VEC>(hzy, &b[2][x - nx]);
+            const T hyx = b[1][x - 1];  // n - 1
+            const T hzx = b[2][x - 1];
+            if (k > 0) {
+                ld_v<T, VEC>(hxz, &bm[0][x]);  // n - Nx*Ny
+                ld_v<T, VEC>(hyz, &bm[1][x]);
+            } else {
+                zero_v<T, VEC>(hxz);
+                zero_v<T, VEC>(hyz);
             }
-        }
-    }
-    for (int k = k0; k < k1; ++k) {
-        T(*b)[kSegMaxNx + kSegCells] = hb[k & 1];
-        T hx[R][VEC], hy[R][VEC], hz[R][VEC];
-        unsigned cd[R][VEC];
-        {
-            const PoolInst<T>& d = seg_desc(dsh);
-            const Geom& g = d.g;
-            const int nx = g.nx;
-            // the Nx cells before the segment, from the old fields (flat index: below p = 0
-            // they wrap into plane k-1; before cell 0 of the grid they are zero); first, so
-            // that no own value is held meanwhile
-            for (int hv = threadIdx.x; hv < nx / VEC; hv += kSegTpb) {
-                const long long m = p0 - nx + (long long)hv * VEC + g.sz * k;
-                T ax[VEC], ay[VEC], az[VEC];
-                if (m >= 0) {
-                    int mi, mj, mk;
-                    cell_of(m, g, mi, mj, mk);
-                    hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, d.mt, m, mi, mj, mk, ax, ay, az, d.code, d.tab);
-                } else {
-                    zero_v<T, VEC>(ax);
-                    zero_v<T, VEC>(ay);
-                    zero_v<T, VEC>(az);
-                }
-                st_v<T, VEC>(&b[0][hv * VEC], ax);
-                st_v<T, VEC>(&b[1][hv * VEC], ay);
-                st_v<T, VEC>(&b[2][hv * VEC], az);
+            T cur[3][VEC];
+            epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, d.mt);
+            unsigned cd[VEC];
+            ld_codes<VEC>(cd, d.code + n);
+            T kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
+            tab_get_v<T, VEC>(d.tab, cd, 1, kx, ky, kz);
+            if constexpr (MODE == 1) {
+                tab_get_v<T, VEC>(d.tab, cd, 2, lx, ly, lz);
+            } else {
+                zero_v<T, VEC>(lx);
+                zero_v<T, VEC>(ly);
+                zero_v<T, VEC>(lz);
             }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int v = threadIdx.x + r * kSegTpb;
-                int i0, j;
-                if (!seg_cell(g, p0, v, VEC, i0, j)) continue;
-                const long long n = p0 + (long long)v * VEC + g.sz * k;
-                if constexpr (FIT_FUSED_PREFETCH > 0) {
-                    constexpr int PF = FIT_FUSED_PREFETCH;
-                    if (k + PF + 1 < g.nz) {
-                        prefetch_l2(Ein + n + (PF + 1) * g.sz);
-                        prefetch_l2(Ein + g.N + n + (PF + 1) * g.sz);
-                    }
-                    if (k + PF < g.nz) {
-                        const long long m = n + PF * g.sz;
-                        prefetch_l2(Ein + 2 * g.N + m);
-                        prefetch_l2(Hin + m);
-                        prefetch_l2(Hin + g.N + m);
-                        prefetch_l2(Hin + 2 * g.N + m);
-                        prefetch_l2(d.code + m);
-                    }
-                }
-                ld_codes<VEC>(cd[r], d.code + n);
-                hpass_eval<T, VEC, true>(Ein, Hin, nullptr, g, d.mt, n, i0, j, k, hx[r], hy[r], hz[r], d.code, d.tab,
-                                         cd[r]);
-                st_v<T, VEC>(Hout + n, hx[r]);
-                st_v<T, VEC>(Hout + g.N + n, hy[r]);
-                st_v<T, VEC>(Hout + 2 * g.N + n, hz[r]);
-                st_v<T, VEC>(&b[0][nx + v * VEC], hx[r]);
-                st_v<T, VEC>(&b[1][nx + v * VEC], hy[r]);
-                st_v<T, VEC>(&b[2][nx + v * VEC], hz[r]);
-            }
-        }
-        __syncthreads();
-        {
-            const PoolInst<T>& d = seg_desc(dsh);
-            const Geom& g = d.g;
-            const int nx = g.nx;
-            StepArgs st{};
-            st.d_step = d.d_step;
-            st.vt_table = d.vt_table;
-            st.vt_len = d.vt_len;
-            const PlaneArgs pl{};
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int v = threadIdx.x + r * kSegTpb;
-                int i0, j;
-                if (!seg_cell(g, p0, v, VEC, i0, j)) continue;
-                const long long n = p0 + (long long)v * VEC + g.sz * k;
-                T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
-                ld_v<T, VEC>(hxy, &b[0][v * VEC]);  // n - Nx
-                ld_v<T, VEC>(hzy, &b[2][v * VEC]);
-                const T hyx = b[1][nx + v * VEC - 1];  // n - 1
-                const T hzx = b[2][nx + v * VEC - 1];
-                if (k > 0) {
-#pragma unroll
-                    for (int e = 0; e < VEC; ++e) {
-                        hxz[e] = px[r][e];
-                        hyz[e] = py[r][e];
-                    }
-                } else {
-                    zero_v<T, VEC>(hxz);
-                    zero_v<T, VEC>(hyz);
-                }
-                T cur[3][VEC];
-                epass_curl<T, VEC>(hx[r], hy[r], hz[r], hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, d.mt);
-                T kx[VEC], ky[VEC], kz[VEC], lx[VEC], ly[VEC], lz[VEC];
-                tab_get_v<T, VEC>(d.tab, cd[r], 1, kx, ky, kz);
-                if constexpr (MODE == 1) {
-                    tab_get_v<T, VEC>(d.tab, cd[r], 2, lx, ly, lz);
-                } else {
-                    zero_v<T, VEC>(lx);
-                    zero_v<T, VEC>(ly);
-                    zero_v<T, VEC>(lz);
-                }
-                T ex[VEC], ey[VEC], ez[VEC];
-                ldg_v<T, VEC>(ex, Ein + n);
-                ldg_v<T, VEC>(ey, Ein + g.N + n);
-                ldg_v<T, VEC>(ez, Ein + 2 * g.N + n);
-                epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, d.J, n, i0, j, k, d.use_cond, g,
-                                           d.beam, pl, st);
-                st_v<T, VEC>(Eout + n, ex);
-                st_v<T, VEC>(Eout + g.N + n, ey);
-                st_v<T, VEC>(Eout + 2 * g.N + n, ez);
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) {
-                    px[r][e] = hx[r][e];
-                    py[r][e] = hy[r][e];
-                }
-            }
+            T ex[VEC], ey[VEC], ez[VEC];
+            ldg_v<T, VEC>(ex, Ein + n);
+            ldg_v<T, VEC>(ey, Ein + g.N + n);
+            ldg_v<T, VEC>(ez, Ein + 2 * g.N + n);
+            epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, d.J, n, i0, j, k, d.use_cond, g,
+                                       d.beam, pl, st);
+            st_v<T, VEC>(Eout + n, ex);
+            st_v<T, VEC>(Eout + g.N + n, ey);
+            st_v<T, VEC>(Eout + 2 * g.N + n, ez);
         }
     }
 }
@@ -2263,7 +2238,7 @@ __device__ __forceinline__ void seg_march(const PoolInst<T>* dsh, const T* __res
 // MINB: CTAs per SM the register budget is sized for (the launch bound).
 template <typename T, int VEC, int MINB>
 __global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable<T>* __restrict__ tab, int dir) {
-    __shared__ __align__(16) T hb[2][3][kSegMaxNx + kSegCells];
+    __shared__ __align__(16) T hb[3][3][kSegWin];
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
     const int ninst = tab->ninst;
@@ -2282,7 +2257,7 @@ __global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable
         if (!run) continue;
         const long long local = w - lo_w;
         const int zr = (int)(local / si.nseg);
-        const long long p0 = (local - (long long)zr * si.nseg) * kSegCells;
+        const long long p0 = (local - (long long)zr * si.nseg) * (kSegWin - si.g.nx);
         const int k0 = zr * si.zlen, k1 = min(si.g.nz, k0 + si.zlen);
         const T* Ein = dir ? si.E2 : si.E;
         const T* Hin = dir ? si.H2 : si.H;

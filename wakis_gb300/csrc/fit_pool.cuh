@@ -51,7 +51,7 @@ struct FitPool {
     int ctas_per_sm = 0;
     int minb[3]{3, 3, 4};          // kernel variant (CTAs per SM of its register budget) per class
     int grid_h[3]{}, grid_e[3]{};  // persistent CTAs of the pass kernels per vector class
-    int fminb[3]{3, 3, 3};         // fused kernel variant (CTAs per SM) per vector width 4, 2, 1
+    int fminb[3]{3, 3, 4};         // fused kernel variant (CTAs per SM) per vector width 4, 2, 1
     int grid_f[3]{};               // persistent CTAs of the fused kernels (4-, 2-, 1-wide vectors)
     int gen = 0;                   // bumped by fit_pool_tune: captured graphs of older variants are stale
     cudaStream_t ps = nullptr;     // every chunk runs here
@@ -230,15 +230,19 @@ struct PoolTune {
     int minb[3], grid_h[3], grid_e[3], fminb[3], grid_f[3], gen;
 };
 
-// the pooled fused kernel of vector width vec, compiled with the register budgets of 2
-// and 3 CTAs per SM (m)
-bool pool_fminb_ok(int m) { return m == 2 || m == 3; }
+// the pooled fused kernel of vector width vec, compiled with the register budgets of m
+// CTAs per SM: vec 4: 2 or 3, vec 2 and 1: 3 or 4
+constexpr int kSegMinb[3][2] = {{2, 3}, {3, 4}, {3, 4}};
+bool pool_fminb_ok(int vec, int m) {
+    const int f = vec == 4 ? 0 : (vec == 2 ? 1 : 2);
+    return m == kSegMinb[f][0] || m == kSegMinb[f][1];
+}
 const void* pool_seg_func(int vec, int m) {
     if (vec == 4)
         return m == 2 ? (const void*)k_step_seg_pool<float, 4, 2> : (const void*)k_step_seg_pool<float, 4, 3>;
     if (vec == 2)
-        return m == 2 ? (const void*)k_step_seg_pool<float, 2, 2> : (const void*)k_step_seg_pool<float, 2, 3>;
-    return m == 2 ? (const void*)k_step_seg_pool<float, 1, 2> : (const void*)k_step_seg_pool<float, 1, 3>;
+        return m == 3 ? (const void*)k_step_seg_pool<float, 2, 3> : (const void*)k_step_seg_pool<float, 2, 4>;
+    return m == 3 ? (const void*)k_step_seg_pool<float, 1, 3> : (const void*)k_step_seg_pool<float, 1, 4>;
 }
 
 // persistent CTAs of the fused kernel of vector width vec with variant m
@@ -628,7 +632,7 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
         r.fused = 1;
         r.E2 = static_cast<float*>(c->E2);
         r.H2 = static_cast<float*>(c->H2);
-        r.nseg = (c->g.sz + kSegCells - 1) / kSegCells;
+        r.nseg = (c->g.sz + (kSegWin - c->g.nx) - 1) / (kSegWin - c->g.nx);
         r.zlen = kSegZlenMax;  // set per chunk by stage_table
         r.ntile = r.nseg * ((c->g.nz + r.zlen - 1) / r.zlen);
     }
@@ -700,9 +704,9 @@ int fit_pool_tune(FitPool* p, int32_t vec, int32_t ctas_per_sm) {
 
 int fit_pool_tune_fused(FitPool* p, int32_t vec, int32_t ctas_per_sm) {
     if (!p || (vec != 4 && vec != 2 && vec != 1)) return FIT_ERR_ARG;
-    if (!pool_fminb_ok(ctas_per_sm)) {
+    if (!pool_fminb_ok(vec, ctas_per_sm)) {
         std::lock_guard<std::mutex> lk(p->mu);
-        p->err = "no compiled fused pool kernel variant for that CTAs per SM (2 or 3)";
+        p->err = "no compiled fused pool kernel variant for that vector width and CTAs per SM";
         return FIT_ERR_ARG;
     }
     const int f = vec == 4 ? 0 : (vec == 2 ? 1 : 2);

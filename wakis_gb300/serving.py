@@ -199,7 +199,7 @@ def solve_alone(req, dtype=np.float32, device=0, dt=None, kernels="auto"):
 
 
 POOL_VARIANTS = {4: (2, 3), 2: (2, 3), 1: (3, 4)}
-POOL_FUSED_VARIANTS = (2, 3)  # CTAs per SM of the pooled fused kernel's compiled register budgets
+POOL_FUSED_VARIANTS = {4: (2, 3), 2: (3, 4), 1: (3, 4)}  # the pooled fused kernel's compiled budgets
 
 
 def run_resident(pool, reqs, kernels="direct"):
@@ -249,7 +249,7 @@ def autotune(pool, calib=None, repeats=1, kernels="direct"):
     out = {}
     for vec, reqs in calib.items():
         rates = {}
-        for minb in (POOL_FUSED_VARIANTS if fused else POOL_VARIANTS[vec]):
+        for minb in (POOL_FUSED_VARIANTS if fused else POOL_VARIANTS)[vec]:
             select(vec, minb)
             best = 0.0
             for _ in range(repeats):
