@@ -773,6 +773,144 @@ __device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict_
                                       mt, b, pl, st, n, i0, j, k, code, tab);
 }
 
+// ---------------------------------------------------------------- cell pairs (odd Nx)
+// Grids with Nx odd have no 2-cell vectors inside rows, but when N is even the flat
+// index splits into pairs (n, n+1), n even, that are 8-byte aligned in every component.
+// A pair reads its own values as pairs and its neighbours at odd offsets one by one, and
+// each of its two cells keeps its own (i, j, k): a pair may straddle two rows (the last
+// cell of a row and the first of the next) or two planes, exactly the flat-index
+// neighbours of the reference's curl, so no warp takes a separate path there.  Each cell
+// gets the inputs the 1-wide kernels give it (hpass_at / epass_at with VEC = 1) and the
+// same arithmetic (hpass_cells / epass_curl / epass_update), hence the same bits.
+__device__ __forceinline__ void pair_cells(long long n, const Geom& g, int (&i)[2], int (&j)[2], int (&k)[2]) {
+    cell_of(n, g, i[0], j[0], k[0]);
+    i[1] = i[0] + 1;
+    j[1] = j[0];
+    k[1] = k[0];
+    if (i[1] == g.nx) {
+        i[1] = 0;
+        if (++j[1] == g.ny) {
+            j[1] = 0;
+            ++k[1];
+        }
+    }
+}
+
+// the two values at p (8-byte aligned for FP32); RO: through the read-only path (inputs
+// the kernel does not write)
+template <typename T, bool RO>
+__device__ __forceinline__ void ld_pair(T (&r)[2], const T* p) {
+    if constexpr (sizeof(T) == 4) {
+        const float2 t = RO ? __ldg(reinterpret_cast<const float2*>(p)) : *reinterpret_cast<const float2*>(p);
+        r[0] = t.x;
+        r[1] = t.y;
+    } else {
+        r[0] = RO ? __ldg(p) : p[0];
+        r[1] = RO ? __ldg(p + 1) : p[1];
+    }
+}
+
+// H pass of the cell pair at even flat index n (coded coefficients)
+template <typename T>
+__device__ __forceinline__ void hpass_pair_at(const T* __restrict__ E, T* __restrict__ H, const Geom& g,
+                                              const Metric<T>& mt, long long n, const unsigned short* __restrict__ code,
+                                              const T* __restrict__ tab) {
+    int i[2], j[2], k[2];
+    pair_cells(n, g, i, j, k);
+    const T* Ex = E;
+    const T* Ey = E + g.N;
+    const T* Ez = E + 2 * g.N;
+    T ex[2], ey[2], ez[2], hx[2], hy[2], hz[2];
+    ld_pair<T, true>(ex, Ex + n);
+    ld_pair<T, true>(ey, Ey + n);
+    ld_pair<T, true>(ez, Ez + n);
+    ld_pair<T, false>(hx, H + n);
+    ld_pair<T, false>(hy, H + g.N + n);
+    ld_pair<T, false>(hz, H + 2 * g.N + n);
+    const unsigned cc = __ldg(reinterpret_cast<const unsigned*>(code + n));
+    T eyn = T(0), ezn = T(0);  // past the pair: (n + 2)
+    if (n + 2 < g.N) {
+        eyn = __ldg(Ey + n + 2);
+        ezn = __ldg(Ez + n + 2);
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const long long m = n + e;
+        const bool yv = (j[e] + 1 < g.ny) || (k[e] + 1 < g.nz);
+        const bool zv = k[e] + 1 < g.nz;
+        T exy[1] = {yv ? __ldg(Ex + m + g.sy) : T(0)}, ezy[1] = {yv ? __ldg(Ez + m + g.sy) : T(0)};
+        T exz[1] = {zv ? __ldg(Ex + m + g.sz) : T(0)}, eyz[1] = {zv ? __ldg(Ey + m + g.sz) : T(0)};
+        T a[1] = {ex[e]}, b[1] = {ey[e]}, c[1] = {ez[e]};
+        T px[1] = {hx[e]}, py[1] = {hy[e]}, pz[1] = {hz[e]};
+        const unsigned cd[1] = {e ? (cc >> 16) : (cc & 0xffffu)};
+        T cx[1], cy[1], cz[1];
+        tab_get_v<T, 1>(tab, cd, 0, cx, cy, cz);
+        hpass_cells<T, 1>(a, b, c, exy, ezy, exz, eyz, e ? eyn : ey[1], e ? ezn : ez[1], px, py, pz, cx, cy, cz, i[e],
+                          j[e], k[e], g, mt);
+        hx[e] = px[0];
+        hy[e] = py[0];
+        hz[e] = pz[0];
+    }
+    st_v<T, 2>(H + n, hx);
+    st_v<T, 2>(H + g.N + n, hy);
+    st_v<T, 2>(H + 2 * g.N + n, hz);
+}
+
+// E pass (MODE 0 or 1, coded coefficients) of the cell pair at even flat index n
+template <typename T, int MODE>
+__device__ __forceinline__ void epass_pair_at(T* __restrict__ E, const T* __restrict__ H, T* __restrict__ J,
+                                              int use_cond, const Geom& g, const Metric<T>& mt, const BeamArgs& b,
+                                              const StepArgs& st, long long n, const unsigned short* __restrict__ code,
+                                              const T* __restrict__ tab) {
+    int i[2], j[2], k[2];
+    pair_cells(n, g, i, j, k);
+    const T* Hx = H;
+    const T* Hy = H + g.N;
+    const T* Hz = H + 2 * g.N;
+    T hx[2], hy[2], hz[2], ex[2], ey[2], ez[2];
+    ld_pair<T, true>(hx, Hx + n);
+    ld_pair<T, true>(hy, Hy + n);
+    ld_pair<T, true>(hz, Hz + n);
+    ld_pair<T, false>(ex, E + n);
+    ld_pair<T, false>(ey, E + g.N + n);
+    ld_pair<T, false>(ez, E + 2 * g.N + n);
+    const unsigned cc = __ldg(reinterpret_cast<const unsigned*>(code + n));
+    T hyp = T(0), hzp = T(0);  // before the pair: (n - 1)
+    if (n > 0) {
+        hyp = __ldg(Hy + n - 1);
+        hzp = __ldg(Hz + n - 1);
+    }
+    const PlaneArgs pl{};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const long long m = n + e;
+        const bool yv = (j[e] > 0) || (k[e] > 0);
+        const bool zv = k[e] > 0;
+        T hxy[1] = {yv ? __ldg(Hx + m - g.sy) : T(0)}, hzy[1] = {yv ? __ldg(Hz + m - g.sy) : T(0)};
+        T hxz[1] = {zv ? __ldg(Hx + m - g.sz) : T(0)}, hyz[1] = {zv ? __ldg(Hy + m - g.sz) : T(0)};
+        T a[1] = {hx[e]}, bb[1] = {hy[e]}, c[1] = {hz[e]};
+        T cur[3][1];
+        epass_curl<T, 1>(a, bb, c, hxy, hzy, hxz, hyz, e ? hy[0] : hyp, e ? hz[0] : hzp, cur, i[e], j[e], k[e], g, mt);
+        const unsigned cd[1] = {e ? (cc >> 16) : (cc & 0xffffu)};
+        T kx[1], ky[1], kz[1], lx[1], ly[1], lz[1];
+        tab_get_v<T, 1>(tab, cd, 1, kx, ky, kz);
+        if constexpr (MODE == 1) {
+            tab_get_v<T, 1>(tab, cd, 2, lx, ly, lz);
+        } else {
+            lx[0] = ly[0] = lz[0] = T(0);
+        }
+        T fx[1] = {ex[e]}, fy[1] = {ey[e]}, fz[1] = {ez[e]};
+        epass_update<T, 1, MODE>(fx, fy, fz, kx, ky, kz, lx, ly, lz, cur, J, m, i[e], j[e], k[e], use_cond, g, b, pl,
+                                 st);
+        ex[e] = fx[0];
+        ey[e] = fy[0];
+        ez[e] = fz[0];
+    }
+    st_v<T, 2>(E + n, ex);
+    st_v<T, 2>(E + g.N + n, ey);
+    st_v<T, 2>(E + 2 * g.N + n, ez);
+}
+
 template <typename T, int VEC, int MODE>
 __global__ void __launch_bounds__(256, 3) k_epass(T* __restrict__ E, const T* __restrict__ H,
                                                const T* __restrict__ ce, const T* __restrict__ cl,
@@ -1945,6 +2083,7 @@ struct PoolInst {
     int use_cond;
     int fused;        // 1: stepped by k_step_seg_pool
     int zlen;         // fused: planes per work item
+    int pair;         // 1-wide class: 1 when N is even, stepped in cell pairs (nvec = N / 2)
     long long nseg;   // fused: plane segments, ceil(Nx*Ny / (kSegWin - Nx))
     const unsigned short* code;  // coded coefficients (nullptr: dense; two-pass classes only)
     const T* tab;
@@ -2036,7 +2175,10 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_hpass_pool(const PoolTable<T
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
     pool_walk<T, VEC>(tab, si, sn, [](const PoolInst<T>& d, long long v) {
-        if (d.code) {
+        if (VEC == 1 && d.pair) {
+            pool_prefetch<T, 2>(d, v, false);
+            hpass_pair_at<T>(d.E, d.H, d.g, d.mt, v * 2, d.code, d.tab);
+        } else if (d.code) {
             pool_prefetch<T, VEC>(d, v, false);
             hpass_at<T, VEC, true>(d.E, d.H, d.ch, d.g, d.mt, v * VEC, d.code, d.tab);
         } else {
@@ -2055,6 +2197,14 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T
         st.vt_table = d.vt_table;
         st.vt_len = d.vt_len;
         const PlaneArgs pl{};
+        if (VEC == 1 && d.pair) {
+            pool_prefetch<T, 2>(d, v, true);
+            if (d.mode == 1)
+                epass_pair_at<T, 1>(d.E, d.H, d.J, d.use_cond, d.g, d.mt, d.beam, st, v * 2, d.code, d.tab);
+            else
+                epass_pair_at<T, 0>(d.E, d.H, d.J, d.use_cond, d.g, d.mt, d.beam, st, v * 2, d.code, d.tab);
+            return;
+        }
         if (d.code) pool_prefetch<T, VEC>(d, v, true);
         if (d.mode == 1 && d.code)
             epass_at<T, VEC, 1, true>(d.E, d.H, d.ce, d.cl, d.J, nullptr, nullptr, d.use_cond, d.g, d.mt, d.beam, pl,

@@ -624,7 +624,9 @@ int fit_pool_submit(FitPool* p, FitCtx* c, int64_t n0, int64_t nsteps, int64_t t
     r.vt_len = c->vt_len;
     r.n_end = n0 + nsteps;
     r.vec = pick_vec(c);
-    r.nvec = c->g.N / r.vec;
+    // odd Nx with N even and coded coefficients: the 1-wide class steps cell pairs
+    r.pair = (r.vec == 1 && c->g.N % 2 == 0 && c->d_code && c->d_tab) ? 1 : 0;
+    r.nvec = r.pair ? c->g.N / 2 : c->g.N / r.vec;
     r.mode = c->use_cond ? 1 : 0;
     r.use_cond = c->use_cond;
     r.ntile = (r.nvec + kPoolTpb - 1) / kPoolTpb;
