@@ -1741,12 +1741,14 @@ __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
 // entries of a step are ordered by s index; the runs of one s index (one accumulator
 // per line) are summed by one thread, the one holding the first of them.
 template <typename T>
-__device__ __forceinline__ void wake_taps(const T* __restrict__ E, const Geom& g, const TapArgs& tp, long long n) {
+__device__ __forceinline__ void wake_taps(const T* __restrict__ E, const Geom& g, const TapArgs& tp, long long n,
+                                          int slice = 0, int slices = 1) {
     if (tp.nlines > 0 && n >= 0 && n < tp.nsteps) {
         const long long r0 = tp.row_ptr[n], r1 = tp.row_ptr[n + 1];
         const long long cnt = (r1 - r0) * tp.nlines;
         const T* Ez = E + 2 * g.N;
-        for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+        // work items t: this block's slice of them, blockDim.x apart
+        for (long long t = threadIdx.x + (long long)slice * blockDim.x; t < cnt; t += (long long)blockDim.x * slices) {
             const long long e = r0 + t / tp.nlines;
             const int l = (int)(t % tp.nlines);
             const int m = tp.ent_m[e];
@@ -2069,7 +2071,8 @@ struct PoolInst {
     T* J;
     BeamArgs beam;
     TapArgs tap;
-    long long* d_step;  // the instance's step counter, advanced by k_prologue_pool
+    long long* d_step;  // the instance's step counter, left at the next step by k_prologue_pool
+    long long n0c;      // the step the instance takes at the chunk's first step
     const double* vt_table;
     long long vt_len;
     long long n_end;  // steps n < n_end are taken
@@ -2100,7 +2103,7 @@ struct PoolTable {
 // descriptor of the instance owning tile t into shared memory, and its current step
 template <typename T>
 __device__ __forceinline__ void pool_fetch(const PoolTable<T>* __restrict__ tab, int ninst, long long t,
-                                           PoolInst<T>* si, long long* step) {
+                                           PoolInst<T>* si, long long* step, int s, double* vt) {
     int lo = 0, hi = ninst - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -2113,7 +2116,12 @@ __device__ __forceinline__ void pool_fetch(const PoolTable<T>* __restrict__ tab,
     const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&tab->inst[lo]);
     unsigned long long* dst = reinterpret_cast<unsigned long long*>(si);
     for (int w = threadIdx.x; w < (int)(sizeof(PoolInst<T>) / 8); w += blockDim.x) dst[w] = src[w];
-    if (threadIdx.x == 0) *step = *tab->inst[lo].d_step - 1;  // the prologue already advanced it
+    if (threadIdx.x == 0) {  // step s of the chunk and the beam's v*t at it
+        const PoolInst<T>& d = tab->inst[lo];
+        const long long n = d.n0c + s;
+        *step = n;
+        *vt = (d.vt_table && n >= 0 && n < d.vt_len) ? d.vt_table[n] : 0.0;
+    }
 }
 
 // Walks the class's tiles in grid-stride order, so the CTAs in flight sweep the flat
@@ -2124,7 +2132,7 @@ __device__ __forceinline__ void pool_fetch(const PoolTable<T>* __restrict__ tab,
 // test is uniform over the CTA, so the barriers around the fetch are too.
 template <typename T, int VEC, typename Body>
 __device__ __forceinline__ void pool_walk(const PoolTable<T>* __restrict__ tab, PoolInst<T>& si, long long& sn,
-                                          Body body) {
+                                          double& svt, int s, Body body) {
     const int ninst = tab->ninst;
     const long long c0 = tab->cls_t0[pool_class(VEC)], c1 = tab->cls_t0[pool_class(VEC) + 1];
     long long lo_t = 0, hi_t = -1;  // tile range of the cached descriptor
@@ -2132,7 +2140,7 @@ __device__ __forceinline__ void pool_walk(const PoolTable<T>* __restrict__ tab, 
     for (long long t = c0 + blockIdx.x; t < c1; t += gridDim.x) {
         if (t >= hi_t) {
             __syncthreads();  // the previous descriptor is no longer read
-            pool_fetch<T>(tab, ninst, t, &si, &sn);
+            pool_fetch<T>(tab, ninst, t, &si, &sn, s, &svt);
             __syncthreads();
             lo_t = si.tile0;
             hi_t = si.tile0 + si.ntile;
@@ -2140,7 +2148,7 @@ __device__ __forceinline__ void pool_walk(const PoolTable<T>* __restrict__ tab, 
         }
         if (run) {
             const long long v = (t - lo_t) * kPoolTpb + threadIdx.x;
-            if (v < si.nvec) body(si, v);
+            if (v < si.nvec) body(si, v, sn, svt);
         }
     }
 }
@@ -2171,10 +2179,11 @@ __device__ __forceinline__ void pool_prefetch(const PoolInst<T>& d, long long v,
 // MINB: CTAs per SM the register budget is sized for (the launch bound); the pool picks
 // one of the compiled variants per vector class.
 template <typename T, int VEC, int MINB>
-__global__ void __launch_bounds__(kPoolTpb, MINB) k_hpass_pool(const PoolTable<T>* __restrict__ tab) {
+__global__ void __launch_bounds__(kPoolTpb, MINB) k_hpass_pool(const PoolTable<T>* __restrict__ tab, int s) {
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
-    pool_walk<T, VEC>(tab, si, sn, [](const PoolInst<T>& d, long long v) {
+    __shared__ double svt;
+    pool_walk<T, VEC>(tab, si, sn, svt, s, [](const PoolInst<T>& d, long long v, long long, double) {
         if (VEC == 1 && d.pair) {
             pool_prefetch<T, 2>(d, v, false);
             hpass_pair_at<T>(d.E, d.H, d.g, d.mt, v * 2, d.code, d.tab);
@@ -2188,14 +2197,14 @@ __global__ void __launch_bounds__(kPoolTpb, MINB) k_hpass_pool(const PoolTable<T
 }
 
 template <typename T, int VEC, int MINB>
-__global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T>* __restrict__ tab) {
+__global__ void __launch_bounds__(kPoolTpb, MINB) k_epass_pool(const PoolTable<T>* __restrict__ tab, int s) {
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
-    pool_walk<T, VEC>(tab, si, sn, [](const PoolInst<T>& d, long long v) {
-        StepArgs st{};
-        st.d_step = d.d_step;
-        st.vt_table = d.vt_table;
-        st.vt_len = d.vt_len;
+    __shared__ double svt;
+    pool_walk<T, VEC>(tab, si, sn, svt, s, [](const PoolInst<T>& d, long long v, long long n, double vt) {
+        StepArgs st{};  // the step and beam position, given
+        st.n = n;
+        st.vt = vt;
         const PlaneArgs pl{};
         if (VEC == 1 && d.pair) {
             pool_prefetch<T, 2>(d, v, true);
@@ -2318,7 +2327,7 @@ __device__ __forceinline__ void seg_hwindow(const PoolInst<T>& d, const T* __res
 template <typename T, int VEC, int MODE>
 __device__ __forceinline__ void seg_march(const PoolInst<T>* dsh, const T* __restrict__ Ein, const T* __restrict__ Hin,
                                           T* __restrict__ Eout, T* __restrict__ Hout, long long p0, int k0, int k1,
-                                          T (*hb)[3][kSegWin]) {
+                                          T (*hb)[3][kSegWin], long long step, double vt) {
     constexpr int R = seg_reps<VEC>();
     if (k0 > 0) seg_hwindow<T, VEC>(seg_desc(dsh), Ein, Hin, Hout, p0, k0 - 1, false, hb);
     for (int k = k0; k < k1; ++k) {
@@ -2329,10 +2338,9 @@ __device__ __forceinline__ void seg_march(const PoolInst<T>* dsh, const T* __res
         const int nx = g.nx;
         T(*b)[kSegWin] = hb[k % 3];
         T(*bm)[kSegWin] = hb[(k + 2) % 3];  // plane k-1
-        StepArgs st{};
-        st.d_step = d.d_step;
-        st.vt_table = d.vt_table;
-        st.vt_len = d.vt_len;
+        StepArgs st{};  // the step and beam position, given
+        st.n = step;
+        st.vt = vt;
         const PlaneArgs pl{};
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -2387,10 +2395,11 @@ __device__ __forceinline__ void seg_march(const PoolInst<T>* dsh, const T* __res
 
 // MINB: CTAs per SM the register budget is sized for (the launch bound).
 template <typename T, int VEC, int MINB>
-__global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable<T>* __restrict__ tab, int dir) {
+__global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable<T>* __restrict__ tab, int dir, int s) {
     __shared__ __align__(16) T hb[3][3][kSegWin];
     __shared__ PoolInst<T> si;
     __shared__ long long sn;
+    __shared__ double svt;
     const int ninst = tab->ninst;
     const long long c0 = tab->cls_t0[pool_fused_class(VEC)], c1 = tab->cls_t0[pool_fused_class(VEC) + 1];
     long long lo_w = 0, hi_w = -1;  // work items of the cached descriptor
@@ -2398,7 +2407,7 @@ __global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable
     for (long long w = c0 + blockIdx.x; w < c1; w += gridDim.x) {
         __syncthreads();  // the previous work item no longer reads hb or si
         if (w >= hi_w) {
-            pool_fetch<T>(tab, ninst, w, &si, &sn);
+            pool_fetch<T>(tab, ninst, w, &si, &sn, s, &svt);
             __syncthreads();
             lo_w = si.tile0;
             hi_w = si.tile0 + si.ntile;
@@ -2414,23 +2423,27 @@ __global__ void __launch_bounds__(kSegTpb, MINB) k_step_seg_pool(const PoolTable
         T* Eout = dir ? si.E : si.E2;
         T* Hout = dir ? si.H : si.H2;
         if (si.mode == 1)
-            seg_march<T, VEC, 1>(&si, Ein, Hin, Eout, Hout, p0, k0, k1, hb);
+            seg_march<T, VEC, 1>(&si, Ein, Hin, Eout, Hout, p0, k0, k1, hb, sn, svt);
         else
-            seg_march<T, VEC, 0>(&si, Ein, Hin, Eout, Hout, p0, k0, k1, hb);
+            seg_march<T, VEC, 0>(&si, Ein, Hin, Eout, Hout, p0, k0, k1, hb, sn, svt);
     }
 }
 
-// one block per table row: wake taps of E^n (read from the buffer holding the state:
-// the second one on odd steps of a fused instance) and the step counter (advanced past
-// the end too, so the passes of this step see n >= n_end and skip the finished instance)
+// kPoolProSlices blocks per table row: wake taps of E^n, step n = n0c + s of the row's
+// instance (read from the buffer holding the state: the second one on odd steps of a
+// fused instance), each block a slice of the step's tap entries; the first block leaves
+// the instance's step counter at n + 1, where a later single-grid run continues.  Nothing
+// in the pool reads the counter: every pass takes its step from the table.
+constexpr int kPoolProSlices = 8;
 template <typename T>
-__global__ void k_prologue_pool(const PoolTable<T>* __restrict__ tab, int dir) {
-    if ((int)blockIdx.x >= tab->ninst) return;
-    const PoolInst<T>& d = tab->inst[blockIdx.x];
-    const long long n = *d.d_step;
-    if (n < d.n_end) wake_taps<T>((d.fused && dir) ? d.E2 : d.E, d.g, d.tap, n);
-    __syncthreads();
-    if (threadIdx.x == 0) *d.d_step = n + 1;
+__global__ void k_prologue_pool(const PoolTable<T>* __restrict__ tab, int dir, int s) {
+    const int row = (int)blockIdx.x / kPoolProSlices, slice = (int)blockIdx.x % kPoolProSlices;
+    if (row >= tab->ninst) return;
+    const PoolInst<T>& d = tab->inst[row];
+    const long long n = d.n0c + s;
+    if (n >= d.n_end) return;
+    wake_taps<T>((d.fused && dir) ? d.E2 : d.E, d.g, d.tap, n, slice, kPoolProSlices);
+    if (slice == 0 && threadIdx.x == 0) *d.d_step = n + 1;
 }
 
 }  // namespace fit

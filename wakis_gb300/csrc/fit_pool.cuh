@@ -175,6 +175,7 @@ int stage_table(FitPool* p, int b, const std::vector<PoolSlot*>& members) {
             if (sc != cls) continue;
             PoolInst<float>& r = t->inst[n++];
             r = s->row;
+            r.n0c = r.n_end - s->nsteps + s->sched;  // the pooled steps are [n_end - nsteps, n_end)
             if (r.fused) {
                 r.zlen = zlen;
                 r.ntile = r.nseg * ((r.g.nz + zlen - 1) / zlen);
@@ -300,15 +301,16 @@ cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraph
     PoolTable<float>* tab = p->d_tab[b];
     for (int s = 0; s < p->chunk && e == cudaSuccess; ++s) {
         int dir = s & 1;
-        void* pro_args[2] = {&tab, &dir};
-        e = add_node(gr, &prev, (const void*)k_prologue_pool<float>, kPoolMaxInst, dim3(256), pro_args);
-        void* pass_args[1] = {&tab};
+        void* pro_args[3] = {&tab, &dir, &s};
+        e = add_node(gr, &prev, (const void*)k_prologue_pool<float>, kPoolMaxInst * kPoolProSlices, dim3(256),
+                     pro_args);
+        void* pass_args[2] = {&tab, &s};
         for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass)
             for (int cls = 0; cls < 3 && e == cudaSuccess; ++cls)
                 if (mask & (1 << cls))
                     e = add_node(gr, &prev, pool_pass_func(cls, t.minb[cls], pass == 1),
                                  pass == 1 ? t.grid_e[cls] : t.grid_h[cls], dim3(kPoolTpb), pass_args);
-        void* fused_args[2] = {&tab, &dir};
+        void* fused_args[3] = {&tab, &dir, &s};
         for (int f = 0; f < 3 && e == cudaSuccess; ++f)
             if (mask & (1 << (3 + f)))
                 e = add_node(gr, &prev, pool_seg_func(4 >> f, t.fminb[f]), t.grid_f[f], dim3(kSegTpb), fused_args);
