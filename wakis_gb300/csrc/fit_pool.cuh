@@ -267,9 +267,15 @@ const void* pool_pass_func(int cls, int m, bool e_pass) {
                   : (m == 3 ? (const void*)k_hpass_pool<float, 1, 3> : (const void*)k_hpass_pool<float, 1, 4>);
 }
 
-// appends one kernel node after *prev (graphs are built node by node, not captured, so
-// building one never interferes with device-wide synchronisation by other threads)
-cudaError_t add_node(cudaGraph_t g, cudaGraphNode_t* prev, const void* func, int grid, dim3 block, void** args) {
+// a kernel node that depends on the non-null nodes of deps (graphs are built node by
+// node, not captured, so building one never interferes with device-wide synchronisation
+// by other threads)
+cudaError_t add_node_after(cudaGraph_t g, cudaGraphNode_t* out, const void* func, int grid, dim3 block, void** args,
+                           const cudaGraphNode_t* deps, int ndeps) {
+    cudaGraphNode_t d[8];
+    int n = 0;
+    for (int i = 0; i < ndeps && n < 8; ++i)
+        if (deps[i]) d[n++] = deps[i];
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(func);
     kp.gridDim = dim3((unsigned)grid);
@@ -277,15 +283,17 @@ cudaError_t add_node(cudaGraph_t g, cudaGraphNode_t* prev, const void* func, int
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
     kp.extra = nullptr;
-    cudaGraphNode_t node = nullptr;
-    cudaError_t e = cudaGraphAddKernelNode(&node, g, *prev ? prev : nullptr, *prev ? 1 : 0, &kp);
-    if (e == cudaSuccess) *prev = node;
-    return e;
+    return cudaGraphAddKernelNode(out, g, n ? d : nullptr, n, &kp);
 }
 
 // the graph of table b with the classes in mask: chunk_steps x [taps + counters, the H
 // pass of each two-pass class present, their E passes, the fused step of each fused
-// class present (direction alternating with the step)]
+// class present (direction alternating with the step)].  The classes hold different
+// solves, so their kernels are independent branches and overlap (one class's last wave
+// with another's work): step s's H pass of a class waits only for that class's E pass
+// of step s-1; an E pass or fused step waits for its H pass (fused: its previous step)
+// and for the step's prologue, which reads the E it overwrites; the prologue waits for
+// the whole previous step (it reads the new E and adds to the tap sums in order).
 cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraphExec_t* out) {
     if (p->graph[b][mask] && p->graph_gen[b][mask] == t.gen) {
         *out = p->graph[b][mask];
@@ -297,23 +305,34 @@ cudaError_t pool_graph(FitPool* p, const PoolTune& t, int b, int mask, cudaGraph
     }
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaGraphCreate(&gr, 0);
-    cudaGraphNode_t prev = nullptr;
     PoolTable<float>* tab = p->d_tab[b];
+    cudaGraphNode_t pro = nullptr, ep[3] = {}, fs[3] = {};  // the previous step's nodes
     for (int s = 0; s < p->chunk && e == cudaSuccess; ++s) {
         int dir = s & 1;
         void* pro_args[3] = {&tab, &dir, &s};
-        e = add_node(gr, &prev, (const void*)k_prologue_pool<float>, kPoolMaxInst * kPoolProSlices, dim3(256),
-                     pro_args);
+        const cudaGraphNode_t pro_deps[7] = {pro, ep[0], ep[1], ep[2], fs[0], fs[1], fs[2]};
+        cudaGraphNode_t pro_s = nullptr;
+        e = add_node_after(gr, &pro_s, (const void*)k_prologue_pool<float>, kPoolMaxInst * kPoolProSlices, dim3(256),
+                           pro_args, pro_deps, 7);
         void* pass_args[2] = {&tab, &s};
-        for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass)
-            for (int cls = 0; cls < 3 && e == cudaSuccess; ++cls)
-                if (mask & (1 << cls))
-                    e = add_node(gr, &prev, pool_pass_func(cls, t.minb[cls], pass == 1),
-                                 pass == 1 ? t.grid_e[cls] : t.grid_h[cls], dim3(kPoolTpb), pass_args);
+        for (int cls = 0; cls < 3 && e == cudaSuccess; ++cls) {
+            if (!(mask & (1 << cls))) continue;
+            cudaGraphNode_t h = nullptr;
+            e = add_node_after(gr, &h, pool_pass_func(cls, t.minb[cls], false), t.grid_h[cls], dim3(kPoolTpb),
+                               pass_args, &ep[cls], 1);
+            const cudaGraphNode_t e_deps[2] = {h, pro_s};
+            if (e == cudaSuccess)
+                e = add_node_after(gr, &ep[cls], pool_pass_func(cls, t.minb[cls], true), t.grid_e[cls],
+                                   dim3(kPoolTpb), pass_args, e_deps, 2);
+        }
         void* fused_args[3] = {&tab, &dir, &s};
-        for (int f = 0; f < 3 && e == cudaSuccess; ++f)
-            if (mask & (1 << (3 + f)))
-                e = add_node(gr, &prev, pool_seg_func(4 >> f, t.fminb[f]), t.grid_f[f], dim3(kSegTpb), fused_args);
+        for (int f = 0; f < 3 && e == cudaSuccess; ++f) {
+            if (!(mask & (1 << (3 + f)))) continue;
+            const cudaGraphNode_t f_deps[2] = {fs[f], pro_s};
+            e = add_node_after(gr, &fs[f], pool_seg_func(4 >> f, t.fminb[f]), t.grid_f[f], dim3(kSegTpb), fused_args,
+                               f_deps, 2);
+        }
+        pro = pro_s;
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph[b][mask], gr, 0);
     if (gr) cudaGraphDestroy(gr);
