@@ -290,6 +290,28 @@ long long coded_ahead(const FitCtx* c, bool e_pass) {
     return occ > 0 ? (long long)c->nsm * occ * 256 : 0;
 }
 
+// the same for the cell-pair kernels (Nx odd, N even)
+template <typename T>
+long long pair_ahead(const FitCtx* c, bool e_pass) {
+    if (!FIT_TWO_PASS_PREFETCH) return 0;
+    static const int occ_h = [] {
+        int o = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_hpass_pair<T>, 256, 0) == cudaSuccess ? o : 0;
+    }();
+    static const int occ_e = [] {
+        int o = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_epass_pair<T, 1>, 256, 0) == cudaSuccess ? o : 0;
+    }();
+    const int occ = e_pass ? occ_e : occ_h;
+    return occ > 0 ? (long long)c->nsm * occ * 256 : 0;
+}
+
+// coded grids with Nx odd and N even step cell pairs instead of single cells
+template <int VEC>
+bool use_pairs(const FitCtx* c) {
+    return VEC == 1 && c->d_code && c->d_tab && c->g.N % 2 == 0;
+}
+
 template <typename T, int VEC>
 void launch_h(FitCtx* c) {
     if (VEC * sizeof(T) == 16 && staged_ok(c)) {
@@ -298,6 +320,11 @@ void launch_h(FitCtx* c) {
         allow_smem(k, sm);
         k<<<c->nsm, kTpbH, sm, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
                                        static_cast<const T*>(c->ch), c->g, metric<T>(c), c->d_err, c->wait_limit);
+    } else if (use_pairs<VEC>(c)) {
+        k_hpass_pair<T><<<grid1d(c->g.N / 2, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E), static_cast<T*>(c->H),
+                                                                     c->g, metric<T>(c), c->d_code,
+                                                                     static_cast<const T*>(c->d_tab),
+                                                                     pair_ahead<T>(c, false));
     } else if (c->d_code) {
         const long long nv = c->g.N / VEC;
         k_hpass_coded<T, VEC><<<grid1d(nv, 256), 256, 0, c->own>>>(static_cast<const T*>(c->E),
@@ -341,6 +368,17 @@ void launch_e(FitCtx* c, int mode, const StepArgs& st) {
     const long long nv = c->g.N / VEC;
     const unsigned nb = grid1d(nv, 256);
     const T* tab = static_cast<const T*>(c->d_tab);
+    if (use_pairs<VEC>(c) && mode != 2) {
+        const unsigned np = grid1d(c->g.N / 2, 256);
+        if (mode == 1)
+            k_epass_pair<T, 1><<<np, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
+                                                       c->d_code, tab, pair_ahead<T>(c, true));
+        else
+            k_epass_pair<T, 0><<<np, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane, st,
+                                                       c->d_code, tab, pair_ahead<T>(c, true));
+        count(c);
+        return;
+    }
     if (c->d_code && mode == 0)
         k_epass_coded<T, VEC, 0><<<nb, 256, 0, c->own>>>(E, H, J, c->use_cond, c->g, metric<T>(c), c->beam, c->plane,
                                                          st, c->d_code, tab, coded_ahead<T, VEC>(c, true));

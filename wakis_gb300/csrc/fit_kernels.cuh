@@ -804,9 +804,10 @@ __device__ __forceinline__ void ld_pair(T (&r)[2], const T* p) {
         const float2 t = RO ? __ldg(reinterpret_cast<const float2*>(p)) : *reinterpret_cast<const float2*>(p);
         r[0] = t.x;
         r[1] = t.y;
-    } else {
-        r[0] = RO ? __ldg(p) : p[0];
-        r[1] = RO ? __ldg(p + 1) : p[1];
+    } else {  // FP64: 16-byte aligned too (n and N even)
+        const double2 t = RO ? __ldg(reinterpret_cast<const double2*>(p)) : *reinterpret_cast<const double2*>(p);
+        r[0] = t.x;
+        r[1] = t.y;
     }
 }
 
@@ -861,7 +862,7 @@ template <typename T, int MODE>
 __device__ __forceinline__ void epass_pair_at(T* __restrict__ E, const T* __restrict__ H, T* __restrict__ J,
                                               int use_cond, const Geom& g, const Metric<T>& mt, const BeamArgs& b,
                                               const StepArgs& st, long long n, const unsigned short* __restrict__ code,
-                                              const T* __restrict__ tab) {
+                                              const T* __restrict__ tab, const PlaneArgs& pl = PlaneArgs{}) {
     int i[2], j[2], k[2];
     pair_cells(n, g, i, j, k);
     const T* Hx = H;
@@ -880,7 +881,6 @@ __device__ __forceinline__ void epass_pair_at(T* __restrict__ E, const T* __rest
         hyp = __ldg(Hy + n - 1);
         hzp = __ldg(Hz + n - 1);
     }
-    const PlaneArgs pl{};
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
         const long long m = n + e;
@@ -942,6 +942,45 @@ __global__ void __launch_bounds__(256, 3) k_epass_coded(T* __restrict__ E, const
     }
     epass_at<T, VEC, MODE, true>(E, H, nullptr, nullptr, J, nullptr, nullptr, use_cond, g, mt, b, pl, st, v * VEC,
                                  code, tab);
+}
+
+// The coded two-pass passes on cell pairs (Nx odd, N even: grids with no 2-cell vectors
+// inside rows).  ahead > 0: the thread first asks L2 for E, H and the codes of the pair
+// `ahead` pairs on, the one a thread of the next resident wave of CTAs works on.
+template <typename T>
+__device__ __forceinline__ void pair_prefetch(const T* E, const T* H, const unsigned short* code, long long N,
+                                              long long v, long long ahead) {
+    if (ahead > 0 && (v + ahead) * 2 < N) {
+        const long long m = (v + ahead) * 2;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            prefetch_l2(E + c * N + m);
+            prefetch_l2(H + c * N + m);
+        }
+        prefetch_l2(code + m);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 4) k_hpass_pair(const T* __restrict__ E, T* __restrict__ H, Geom g,
+                                                    Metric<T> mt, const unsigned short* __restrict__ code,
+                                                    const T* __restrict__ tab, long long ahead) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.N / 2) return;
+    pair_prefetch<T>(E, H, code, g.N, v, ahead);
+    hpass_pair_at<T>(E, H, g, mt, v * 2, code, tab);
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256, 4) k_epass_pair(T* __restrict__ E, const T* __restrict__ H,
+                                                    T* __restrict__ J, int use_cond, Geom g, Metric<T> mt,
+                                                    BeamArgs b, PlaneArgs pl, StepArgs st,
+                                                    const unsigned short* __restrict__ code,
+                                                    const T* __restrict__ tab, long long ahead) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.N / 2) return;
+    pair_prefetch<T>(E, H, code, g.N, v, ahead);
+    epass_pair_at<T, MODE>(E, H, J, use_cond, g, mt, b, st, v * 2, code, tab, pl);
 }
 
 // ---------------------------------------------------------------- fused step (2.5-D)
