@@ -100,11 +100,11 @@ def test_coded_coefficients_equal_dense(name, kernels, tmp_path, monkeypatch):
         np.testing.assert_array_equal(np.asarray(coded[k]), np.asarray(v), err_msg=f"{name}:{k}")
 
 
-def _random_field_solver(x, y, z, dtype, codes, bcs=(["pec", "pmc", "pec"], ["pml", "pec", "pmc"])):
+def _random_field_solver(x, y, z, dtype, codes, bcs=(["pec", "pmc", "pec"], ["pml", "pec", "pmc"]), bg=(1.0, 1.0)):
     import wakis_gb300 as wg
     blk = lambda X, Y, Z: (np.abs(X) < 0.4) & (Z > 0.3) & (Z < 1.1)
     grid = wg.GridFIT3D(x=x, y=y, z=z, stl_solids={"blk": blk}, stl_materials={"blk": [2.0, 1.0, 50.0]}, verbose=0)
-    s = wg.SolverFIT3D(grid, cfln=0.5, bc_low=bcs[0], bc_high=bcs[1], use_stl=True, bg=[1.0, 1.0], dtype=dtype,
+    s = wg.SolverFIT3D(grid, cfln=0.5, bc_low=bcs[0], bc_high=bcs[1], use_stl=True, bg=list(bg), dtype=dtype,
                        n_pml=4, verbose=0)
     s.kernels = "fused"
     s.coefficient_codes = codes
@@ -204,3 +204,34 @@ def test_tma_staging_rejected_where_it_does_not_apply():
     with pytest.raises(nat.FitError):
         s2._ctx.call("fit_set_fused_staging", 1, 1)
     assert isinstance(s2, wg.SolverFIT3D)
+
+
+# ---------------------------------------------------------------- cell pairs
+_GROUP_BCS = [(["pmc", "periodic", "pec"], ["pec", "periodic", "pml"]),
+              (["periodic", "periodic", "periodic"], ["periodic", "periodic", "periodic"]),
+              (["pec", "pmc", "pec"], ["pml", "pec", "pmc"])]
+
+
+@pytest.mark.parametrize("dtype,nx,ny,nz,bcs", [
+    (np.float32, 17, 13, 40, 0), (np.float32, 17, 13, 40, 1), (np.float32, 17, 13, 40, 2),
+    (np.float64, 17, 13, 40, 0), (np.float64, 17, 13, 40, 1), (np.float64, 17, 13, 40, 2),
+    (np.float32, 15, 7, 20, 2), (np.float32, 1, 5, 8, 1), (np.float64, 3, 3, 6, 1)])
+def test_cell_groups_equal_row_vectors(dtype, nx, ny, nz, bcs):
+    """The coded two-pass passes on flat-index cell pairs (Nx odd, N even) against the
+    dense two-pass passes on single cells: random E, H, lossy blocks, every face kind
+    including the periodic row and plane crossings a pair straddles (Nx = 1: every pair
+    spans two rows), an odd step count; bit for bit."""
+    x = np.linspace(-1, 1, nx + 1)
+    y = np.linspace(-0.8, 0.7, ny + 1)
+    z = np.linspace(-2, 2, nz + 1)
+    out = {}
+    for codes in (True, False):
+        # a lossy background (tau = eps/sigma above dt) keeps every cell conductive, so tiny
+        # grids that the block misses still run the loss-factor step
+        s = _random_field_solver(x, y, z, dtype, codes, bcs=_GROUP_BCS[bcs], bg=(1.5, 1.0, 1e-3))
+        s.kernels = "direct"
+        s.emsolve(21)
+        out[codes] = (s.E.numpy(), s.H.numpy(), s.J.numpy(), s.coefficient_code_count)
+    assert out[True][3] > 0 and out[False][3] == 0
+    for a, b, k in zip(out[True][:3], out[False][:3], "EHJ"):
+        np.testing.assert_array_equal(a, b, err_msg=k)
