@@ -359,7 +359,7 @@ FIT_API int fit_pool_cancel(FitPool *pool, int64_t tag);
 FIT_API int fit_pool_stats(FitPool *pool, FitPoolStats *out);
 /* Chooses the pass kernels of one vector-width class (vec = 4, 2 or 1 cells per vector,
  * the widest that divides Nx): ctas_per_sm names the compiled variant by the CTAs per SM
- * its register budget is sized for (vec 4: 2 or 3, vec 2: 2 or 3, vec 1: 3 or 4; the
+ * its register budget is sized for (vec 4: 2 or 3, vec 2: 3 or 4, vec 1: 3 or 4; the
  * defaults are 3, 3 and 4).  Applies from the next chunk; graphs of the old variant are recaptured.
  * The serving layer's autotuner times the variants on the requests' own grids. */
 FIT_API int fit_pool_tune(FitPool *pool, int32_t vec, int32_t ctas_per_sm);

@@ -199,7 +199,7 @@ bool pool_fused_ok(const FitCtx* c, int mode) {
 }
 
 // compiled variants: launch bound (CTAs per SM) choices per vector class
-constexpr int kPoolMinb[3][2] = {{2, 3}, {2, 3}, {3, 4}};
+constexpr int kPoolMinb[3][2] = {{2, 3}, {3, 4}, {3, 4}};
 
 bool pool_minb_ok(int cls, int minb) { return minb == kPoolMinb[cls][0] || minb == kPoolMinb[cls][1]; }
 
@@ -217,7 +217,7 @@ cudaError_t pool_grids(int nsm, int cls, int minb, int ctas_per_sm, int* gh, int
     if (cls == 0)
         e = minb == 2 ? pool_occupancy<4, 2>(&oh, &oe) : pool_occupancy<4, 3>(&oh, &oe);
     else if (cls == 1)
-        e = minb == 2 ? pool_occupancy<2, 2>(&oh, &oe) : pool_occupancy<2, 3>(&oh, &oe);
+        e = minb == 3 ? pool_occupancy<2, 3>(&oh, &oe) : pool_occupancy<2, 4>(&oh, &oe);
     else
         e = minb == 3 ? pool_occupancy<1, 3>(&oh, &oe) : pool_occupancy<1, 4>(&oh, &oe);
     oh = std::max(oh, 1);
@@ -261,8 +261,8 @@ const void* pool_pass_func(int cls, int m, bool e_pass) {
         return e_pass ? (m == 2 ? (const void*)k_epass_pool<float, 4, 2> : (const void*)k_epass_pool<float, 4, 3>)
                       : (m == 2 ? (const void*)k_hpass_pool<float, 4, 2> : (const void*)k_hpass_pool<float, 4, 3>);
     if (cls == 1)
-        return e_pass ? (m == 2 ? (const void*)k_epass_pool<float, 2, 2> : (const void*)k_epass_pool<float, 2, 3>)
-                      : (m == 2 ? (const void*)k_hpass_pool<float, 2, 2> : (const void*)k_hpass_pool<float, 2, 3>);
+        return e_pass ? (m == 3 ? (const void*)k_epass_pool<float, 2, 3> : (const void*)k_epass_pool<float, 2, 4>)
+                      : (m == 3 ? (const void*)k_hpass_pool<float, 2, 3> : (const void*)k_hpass_pool<float, 2, 4>);
     return e_pass ? (m == 3 ? (const void*)k_epass_pool<float, 1, 3> : (const void*)k_epass_pool<float, 1, 4>)
                   : (m == 3 ? (const void*)k_hpass_pool<float, 1, 3> : (const void*)k_hpass_pool<float, 1, 4>);
 }

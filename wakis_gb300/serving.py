@@ -198,7 +198,7 @@ def solve_alone(req, dtype=np.float32, device=0, dt=None, kernels="auto"):
     return out
 
 
-POOL_VARIANTS = {4: (2, 3), 2: (2, 3), 1: (3, 4)}
+POOL_VARIANTS = {4: (2, 3), 2: (3, 4), 1: (3, 4)}
 POOL_FUSED_VARIANTS = {4: (2, 3), 2: (3, 4), 1: (3, 4)}  # the pooled fused kernel's compiled budgets
 
 
