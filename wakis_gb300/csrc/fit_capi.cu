@@ -269,7 +269,8 @@ void allow_smem(KernelPtr k, size_t bytes) {
 
 // vectors between a thread and its counterpart in the next resident wave of CTAs of a
 // coded two-pass kernel (its L2 prefetch distance); 0 turns the prefetch off.  The
-// 1-wide kernels go without: their prefetch did not pay in the serving pool.
+// single-cell kernels go without: their prefetch did not pay in the serving pool (the
+// cell-pair kernels have their own, pair_ahead).
 #ifndef FIT_TWO_PASS_PREFETCH
 #define FIT_TWO_PASS_PREFETCH 1
 #endif

@@ -2192,11 +2192,11 @@ __device__ __forceinline__ void pool_walk(const PoolTable<T>* __restrict__ tab, 
     }
 }
 
-// Coded two-pass classes with 2- and 4-wide vectors: the first-touch data of the same
-// thread's vector in the next grid-stride tile (E, H and the code) is requested into L2
-// while this tile is worked on.  Measured on the calibration grids (all resident, G
-// cell-updates/s): vec 4 53.7 -> 57.7, vec 2 49.6 -> 60.9; vec 1 39.4 -> 38.2, so the
-// 1-wide class does without.
+// Coded two-pass classes with 2- and 4-wide vectors and cell pairs: the first-touch data
+// of the same thread's vector (or pair) in the next grid-stride tile (E, H and the code)
+// is requested into L2 while this tile is worked on.  Measured on the calibration grids
+// (all resident, G cell-updates/s): vec 4 53.7 -> 57.7, vec 2 49.6 -> 60.9; single cells
+// 39.4 -> 38.2, so the 1-wide class without pairs (N odd) does without.
 #ifndef FIT_POOL_PREFETCH
 #define FIT_POOL_PREFETCH 1
 #endif
