@@ -778,8 +778,9 @@ int fit_ctx_create(const FitGridDesc* d, FitCtx** out) {
         return fail(nullptr, FIT_ERR_ARG, "grid dimensions must be >= 1 (got %lld x %lld x %lld)",
                     (long long)d->nx, (long long)d->ny, (long long)d->nz);
     const long long N = d->nx * d->ny * d->nz;
-    if (N >= (1LL << 31))
-        return fail(nullptr, FIT_ERR_ARG, "grid too large: N = %lld cells (limit 2^31 - 1)", N);
+    // the kernels address cells by 32-bit offsets up to N + Nx*Ny from a component's start
+    if (N + d->nx * d->ny >= (1LL << 31))
+        return fail(nullptr, FIT_ERR_ARG, "grid too large: N = %lld cells (limit N + Nx*Ny < 2^31)", N);
     if (d->dtype != FIT_F32 && d->dtype != FIT_F64) return fail(nullptr, FIT_ERR_ARG, "dtype must be FIT_F32 or FIT_F64");
     for (int a = 0; a < 3; ++a)
         if (d->bc_lo[a] < 0 || d->bc_lo[a] > 4 || d->bc_hi[a] < 0 || d->bc_hi[a] > 4)

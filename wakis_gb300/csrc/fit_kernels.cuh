@@ -537,52 +537,57 @@ __device__ __forceinline__ void hpass_eval(const T* __restrict__ E, const T* H, 
                                            T (&hx)[VEC], T (&hy)[VEC], T (&hz)[VEC],
                                            const unsigned short* __restrict__ code = nullptr,
                                            const T* __restrict__ tab = nullptr, const unsigned* pre = nullptr) {
-    const T* Ex = E;
-    const T* Ey = E + g.N;
-    const T* Ez = E + 2 * g.N;
+    // 32-bit offsets from per-component pointers (n + Nx*Ny < 2^31 is checked on the
+    // host): one multiply-add per address instead of 64-bit index arithmetic
+    const int ni = (int)n, N = (int)g.N, sy = (int)g.sy, sz = (int)g.sz;
+    const T* Ex = E + ni;
+    const T* Ey = Ex + N;
+    const T* Ez = Ey + N;
     T ex[VEC], ey[VEC], ez[VEC];
-    ldg_v<T, VEC>(ex, Ex + n);
-    ldg_v<T, VEC>(ey, Ey + n);
-    ldg_v<T, VEC>(ez, Ez + n);
+    ldg_v<T, VEC>(ex, Ex);
+    ldg_v<T, VEC>(ey, Ey);
+    ldg_v<T, VEC>(ez, Ez);
     const bool yv = (j + 1 < g.ny) || (k + 1 < g.nz);
     const bool zv = (k + 1 < g.nz);
     T exy[VEC], ezy[VEC], exz[VEC], eyz[VEC];
     if (yv) {
-        ldg_v<T, VEC>(exy, Ex + n + g.sy);
-        ldg_v<T, VEC>(ezy, Ez + n + g.sy);
+        ldg_v<T, VEC>(exy, Ex + sy);
+        ldg_v<T, VEC>(ezy, Ez + sy);
     } else {
         zero_v<T, VEC>(exy);
         zero_v<T, VEC>(ezy);
     }
     if (zv) {
-        ldg_v<T, VEC>(exz, Ex + n + g.sz);
-        ldg_v<T, VEC>(eyz, Ey + n + g.sz);
+        ldg_v<T, VEC>(exz, Ex + sz);
+        ldg_v<T, VEC>(eyz, Ey + sz);
     } else {
         zero_v<T, VEC>(exz);
         zero_v<T, VEC>(eyz);
     }
     T eyx = T(0), ezx = T(0);
-    if (n + VEC < g.N) {
-        eyx = __ldg(Ey + n + VEC);
-        ezx = __ldg(Ez + n + VEC);
+    if (ni + VEC < N) {
+        eyx = __ldg(Ey + VEC);
+        ezx = __ldg(Ez + VEC);
     }
     T cx[VEC], cy[VEC], cz[VEC];
-    ld_v<T, VEC>(hx, H + n);
-    ld_v<T, VEC>(hy, H + g.N + n);
-    ld_v<T, VEC>(hz, H + 2 * g.N + n);
+    const T* Hn = H + ni;
+    ld_v<T, VEC>(hx, Hn);
+    ld_v<T, VEC>(hy, Hn + N);
+    ld_v<T, VEC>(hz, Hn + N + N);
     if constexpr (CODED) {
         unsigned cd[VEC];
         if (pre) {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) cd[e] = pre[e];
         } else {
-            ld_codes<VEC>(cd, code + n);
+            ld_codes<VEC>(cd, code + ni);
         }
         tab_get_v<T, VEC>(tab, cd, 0, cx, cy, cz);
     } else {
-        ldg_v<T, VEC>(cx, ch + n);
-        ldg_v<T, VEC>(cy, ch + g.N + n);
-        ldg_v<T, VEC>(cz, ch + 2 * g.N + n);
+        const T* cn = ch + ni;
+        ldg_v<T, VEC>(cx, cn);
+        ldg_v<T, VEC>(cy, cn + N);
+        ldg_v<T, VEC>(cz, cn + N + N);
     }
     hpass_cells<T, VEC>(ex, ey, ez, exy, ezy, exz, eyz, eyx, ezx, hx, hy, hz, cx, cy, cz, i0, j, k, g, mt);
 }
@@ -655,16 +660,19 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
     epass_curl<T, VEC>(hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, cur, i0, j, k, g, mt);
     T ex[VEC], ey[VEC], ez[VEC], kx[VEC], ky[VEC], kz[VEC];
     [[maybe_unused]] unsigned cd[VEC];
-    ld_v<T, VEC>(ex, Esrc + n);
-    ld_v<T, VEC>(ey, Esrc + g.N + n);
-    ld_v<T, VEC>(ez, Esrc + 2 * g.N + n);
+    const int ni = (int)n, N32 = (int)g.N;  // 32-bit offsets, as in hpass_eval
+    const T* Es = Esrc + ni;
+    ld_v<T, VEC>(ex, Es);
+    ld_v<T, VEC>(ey, Es + N32);
+    ld_v<T, VEC>(ez, Es + N32 + N32);
     if constexpr (CODED) {
-        ld_codes<VEC>(cd, code + n);
+        ld_codes<VEC>(cd, code + ni);
         tab_get_v<T, VEC>(tab, cd, 1, kx, ky, kz);
     } else {
-        ldg_v<T, VEC>(kx, ce + n);
-        ldg_v<T, VEC>(ky, ce + g.N + n);
-        ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+        const T* cen = ce + ni;
+        ldg_v<T, VEC>(kx, cen);
+        ldg_v<T, VEC>(ky, cen + N32);
+        ldg_v<T, VEC>(kz, cen + N32 + N32);
     }
     if constexpr (MODE == 2) {
         const bool on_line = b.active && (j == b.iys) && (b.ixs >= i0) && (b.ixs < i0 + VEC);
@@ -715,9 +723,10 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
         if constexpr (MODE == 1 && CODED) {
             tab_get_v<T, VEC>(tab, cd, 2, lx, ly, lz);
         } else if constexpr (MODE == 1) {
-            ldg_v<T, VEC>(lx, cl + n);
-            ldg_v<T, VEC>(ly, cl + g.N + n);
-            ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+            const T* cln = cl + ni;
+            ldg_v<T, VEC>(lx, cln);
+            ldg_v<T, VEC>(ly, cln + N32);
+            ldg_v<T, VEC>(lz, cln + N32 + N32);
         } else {
             zero_v<T, VEC>(lx);
             zero_v<T, VEC>(ly);
@@ -725,9 +734,10 @@ __device__ __forceinline__ void epass_finish(const T* Esrc, T* Edst, const T (&h
         }
         epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, J, n, i0, j, k, use_cond, g, b, pl, st);
     }
-    st_v<T, VEC>(Edst + n, ex);
-    st_v<T, VEC>(Edst + g.N + n, ey);
-    st_v<T, VEC>(Edst + 2 * g.N + n, ez);
+    T* Ed = Edst + ni;
+    st_v<T, VEC>(Ed, ex);
+    st_v<T, VEC>(Ed + N32, ey);
+    st_v<T, VEC>(Ed + N32 + N32, ez);
 }
 
 
@@ -740,34 +750,35 @@ __device__ __forceinline__ void epass_at(T* __restrict__ E, const T* __restrict_
                                          const T* __restrict__ tab = nullptr) {
     int i0, j, k;
     cell_of(n, g, i0, j, k);
-    const T* Hx = H;
-    const T* Hy = H + g.N;
-    const T* Hz = H + 2 * g.N;
+    const int ni = (int)n, N32 = (int)g.N, sy = (int)g.sy, sz = (int)g.sz;  // 32-bit offsets
+    const T* Hx = H + ni;
+    const T* Hy = Hx + N32;
+    const T* Hz = Hy + N32;
     T hx[VEC], hy[VEC], hz[VEC];
-    ldg_v<T, VEC>(hx, Hx + n);
-    ldg_v<T, VEC>(hy, Hy + n);
-    ldg_v<T, VEC>(hz, Hz + n);
+    ldg_v<T, VEC>(hx, Hx);
+    ldg_v<T, VEC>(hy, Hy);
+    ldg_v<T, VEC>(hz, Hz);
     const bool yv = (j > 0) || (k > 0);
     const bool zv = (k > 0);
     T hxy[VEC], hzy[VEC], hxz[VEC], hyz[VEC];
     if (yv) {
-        ldg_v<T, VEC>(hxy, Hx + n - g.sy);
-        ldg_v<T, VEC>(hzy, Hz + n - g.sy);
+        ldg_v<T, VEC>(hxy, Hx - sy);
+        ldg_v<T, VEC>(hzy, Hz - sy);
     } else {
         zero_v<T, VEC>(hxy);
         zero_v<T, VEC>(hzy);
     }
     if (zv) {
-        ldg_v<T, VEC>(hxz, Hx + n - g.sz);
-        ldg_v<T, VEC>(hyz, Hy + n - g.sz);
+        ldg_v<T, VEC>(hxz, Hx - sz);
+        ldg_v<T, VEC>(hyz, Hy - sz);
     } else {
         zero_v<T, VEC>(hxz);
         zero_v<T, VEC>(hyz);
     }
     T hyx = T(0), hzx = T(0);
-    if (n > 0) {
-        hyx = __ldg(Hy + n - 1);
-        hzx = __ldg(Hz + n - 1);
+    if (ni > 0) {
+        hyx = __ldg(Hy - 1);
+        hzx = __ldg(Hz - 1);
     }
     epass_finish<T, VEC, MODE, CODED>(E, E, hx, hy, hz, hxy, hzy, hxz, hyz, hyx, hzx, ce, cl, J, cj, sg, use_cond, g,
                                       mt, b, pl, st, n, i0, j, k, code, tab);
@@ -1099,37 +1110,43 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
             // the E update's coefficients do not depend on the new H: load them first so
             // their latency overlaps the H update and the barrier (coded: the codes; the
             // table entries are L1 hits, read after the barrier)
+            const int ni = (int)n, N32 = (int)g.N, sz32 = (int)g.sz;  // 32-bit offsets, as in hpass_eval
             if constexpr (CODED && FIT_FUSED_PREFETCH > 0) {
                 constexpr int PF = FIT_FUSED_PREFETCH;
+                const T* Ep = Ein + ni;
                 if (k + PF + 1 < g.nz) {
-                    prefetch_l2(Ein + n + (PF + 1) * g.sz);
-                    prefetch_l2(Ein + g.N + n + (PF + 1) * g.sz);
+                    prefetch_l2(Ep + (PF + 1) * sz32);
+                    prefetch_l2(Ep + N32 + (PF + 1) * sz32);
                 }
                 if (k + PF < g.nz) {
-                    const long long m = n + PF * g.sz;
-                    prefetch_l2(Ein + 2 * g.N + m);
-                    prefetch_l2(Hin + m);
-                    prefetch_l2(Hin + g.N + m);
-                    prefetch_l2(Hin + 2 * g.N + m);
+                    const int m = ni + PF * sz32;
+                    const T* Hp = Hin + m;
+                    prefetch_l2(Ein + m + N32 + N32);
+                    prefetch_l2(Hp);
+                    prefetch_l2(Hp + N32);
+                    prefetch_l2(Hp + N32 + N32);
                     prefetch_l2(code + m);
                 }
             }
             if constexpr (CODED) {
-                ld_codes<VEC>(cd, code + n);
+                ld_codes<VEC>(cd, code + ni);
             } else {
-                ldg_v<T, VEC>(kx, ce + n);
-                ldg_v<T, VEC>(ky, ce + g.N + n);
-                ldg_v<T, VEC>(kz, ce + 2 * g.N + n);
+                const T* cen = ce + ni;
+                ldg_v<T, VEC>(kx, cen);
+                ldg_v<T, VEC>(ky, cen + N32);
+                ldg_v<T, VEC>(kz, cen + N32 + N32);
                 if constexpr (MODE == 1) {
-                    ldg_v<T, VEC>(lx, cl + n);
-                    ldg_v<T, VEC>(ly, cl + g.N + n);
-                    ldg_v<T, VEC>(lz, cl + 2 * g.N + n);
+                    const T* cln = cl + ni;
+                    ldg_v<T, VEC>(lx, cln);
+                    ldg_v<T, VEC>(ly, cln + N32);
+                    ldg_v<T, VEC>(lz, cln + N32 + N32);
                 }
             }
             hpass_eval<T, VEC, CODED>(Ein, Hin, ch, g, mt, n, i0, j, k, hx, hy, hz, code, tab, cd);
-            st_v<T, VEC>(Hout + n, hx);
-            st_v<T, VEC>(Hout + g.N + n, hy);
-            st_v<T, VEC>(Hout + 2 * g.N + n, hz);
+            T* Ho = Hout + ni;
+            st_v<T, VEC>(Ho, hx);
+            st_v<T, VEC>(Ho + N32, hy);
+            st_v<T, VEC>(Ho + N32 + N32, hz);
 #pragma unroll
             for (int e = 0; e < VEC; ++e) {
                 sm.h[bc][0][ty + 1][xo + e] = hx[e];
@@ -1164,13 +1181,16 @@ __device__ __forceinline__ void fused_march(const T* __restrict__ Ein, const T* 
                 if constexpr (MODE == 1) tab_get_v<T, VEC>(tab, cd, 2, lx, ly, lz);
             }
             T ex[VEC], ey[VEC], ez[VEC];
-            ldg_v<T, VEC>(ex, Ein + n);
-            ldg_v<T, VEC>(ey, Ein + g.N + n);
-            ldg_v<T, VEC>(ez, Ein + 2 * g.N + n);
+            const int ni = (int)n, N32 = (int)g.N;
+            const T* Ei = Ein + ni;
+            ldg_v<T, VEC>(ex, Ei);
+            ldg_v<T, VEC>(ey, Ei + N32);
+            ldg_v<T, VEC>(ez, Ei + N32 + N32);
             epass_update<T, VEC, MODE>(ex, ey, ez, kx, ky, kz, lx, ly, lz, cur, J, n, i0, j, k, use_cond, g, b, pl, st);
-            st_v<T, VEC>(Eout + n, ex);
-            st_v<T, VEC>(Eout + g.N + n, ey);
-            st_v<T, VEC>(Eout + 2 * g.N + n, ez);
+            T* Eo = Eout + ni;
+            st_v<T, VEC>(Eo, ex);
+            st_v<T, VEC>(Eo + N32, ey);
+            st_v<T, VEC>(Eo + N32 + N32, ez);
         }
     }
 }
