@@ -70,7 +70,9 @@ typedef struct FitGridDesc {
 } FitGridDesc;
 
 /* Context lifetime.  Replaces the operator assembly of SolverFIT3D.__init__
- * (wakis/solverFIT3D.py:203-227, 337-344): no sparse matrix is built. */
+ * (wakis/solverFIT3D.py:203-227, 337-344): no sparse matrix is built.  Grids with
+ * N + Nx*Ny >= 2^31 (N = Nx*Ny*Nz) are refused with FIT_ERR_ARG: the kernels address
+ * cells by 32-bit offsets within a field component. */
 FIT_API int fit_ctx_create(const FitGridDesc *desc, FitCtx **out);
 FIT_API int fit_ctx_destroy(FitCtx *ctx);
 /* Copies the last error message (NUL terminated, truncated to len); ctx may be NULL
