@@ -445,8 +445,8 @@ def run_ours(args, rank, world):
 
 
 def serving_summary(args, peak):
-    """The served path, measured in the default run on one GPU (BASELINE metric, second
-    half): the 64-request cavity sweep (cube 20-60 mm, n 48-160, default_rng(seed=3)),
+    """The served path, measured in the default run on one GPU (the second half of the
+    metric: served solves/h and p99): the 64-request cavity sweep (cube 20-60 mm, n 48-160, default_rng(seed=3)),
     arriving as a Poisson stream at which the 4 GB memory budget binds, served in FP32 by
     the pool with continuous batching (two-pass kernel variants chosen by the autotuner on
     calibration grids); the pool's throughput with every request resident, over the first
