@@ -214,10 +214,10 @@ def cpu_sample_rate(nz_slab=16, steps=20, budget_s=25.0, barrier=None):
 
 
 # ----------------------------------------------------------------------------- runs
-def run_cpu_configs(args):
+def run_cpu_workloads(args):
     """The CPU oracle (scipy CSR leapfrog, the reference's algorithm, one thread) on the
-    config 0, 1 and 2 grids in FP64 and FP32: Mcell-updates/s over --cpu-steps steps after
-    one warm-up step (random fields), and the config-0 time-to-impedance (its whole
+    60x60x120 cavity, 128x128x256 lossy cavity and 256^3 sphere grids in FP64 and FP32: Mcell-updates/s over --cpu-steps steps after
+    one warm-up step (random fields), and the 60x60x120 cavity's time-to-impedance (its whole
     FP64 wakesolve, set-up included).  Prints one JSON line."""
     for p in (os.path.join(ROOT, "tests"), os.path.join(ROOT, "tests", "golden")):
         if p not in sys.path:
@@ -225,10 +225,10 @@ def run_cpu_configs(args):
     import cases as C
     from oracle_runner import oracle_solver, run_oracle_case
     rates = {}
-    for name in ("config0", "config1a", "config2"):
+    for name in ("cavity_60x60x120", "lossy_cavity_128x128x256", "sphere_packet_256"):
         for dt in ("float64", "float32"):
             t0 = time.perf_counter()
-            s = oracle_solver(dict(C.CONFIGS[name], dtype=dt))
+            s = oracle_solver(dict(C.WORKLOADS[name], dtype=dt))
             setup = time.perf_counter() - t0
             rng = np.random.default_rng(0)
             s.E[:] = rng.standard_normal(s.E.size).astype(s.E.dtype)
@@ -242,12 +242,12 @@ def run_cpu_configs(args):
                                      "operator_setup_s": setup}
             del s
     t0 = time.perf_counter()
-    r = run_oracle_case("config0", case=C.CONFIGS["config0"])
+    r = run_oracle_case("cavity_60x60x120", case=C.WORKLOADS["cavity_60x60x120"])
     tti = time.perf_counter() - t0
-    print(json.dumps({"mode": "cpu_configs", "impl": "oracle (scipy CSR, one thread)", "threads": 1,
+    print(json.dumps({"mode": "cpu_workloads", "impl": "oracle (scipy CSR, one thread)", "threads": 1,
                       "host_cpus": os.cpu_count(), "rates": rates,
-                      "config0_time_to_impedance": {"seconds": tti, "steps": int(r["Nt"]),
-                                                    "what": "FP64 wakesolve of config 0 through the oracle, "
+                      "cavity_60x60x120_time_to_impedance": {"seconds": tti, "steps": int(r["Nt"]),
+                                                    "what": "FP64 wakesolve of the 60x60x120 cavity through the oracle, "
                                                             "grid and operator set-up included"}}), flush=True)
 
 
@@ -258,7 +258,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "Mcell-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (analytic pillbox geometry)",
-            "config": {"workload": "cfg4 pillbox 512x512x1024 FP32 (bounded z-slab sample on the host)"},
+            "config": {"workload": "pillbox 512x512x1024 FP32 (bounded z-slab sample on the host)"},
             "cpu_baseline": {"value": rate, "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": rate, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -342,7 +342,7 @@ def run_ours(args, rank, world):
     ach_e = bytes_e * N / (kt[1] / 1e3) / 1e9
     ach_h = bytes_h * N / (kt[0] / 1e3) / 1e9
     ach_step = BYTES_STEP_MODEL * N / (ms / K / 1e3) / 1e9
-    traffic = profile_traffic("epass_coded_cfg4_ncu.md" if coded else "epass_cfg4_ncu.md")
+    traffic = profile_traffic("epass_coded_pillbox_ncu.md" if coded else "epass_pillbox_ncu.md")
     fused = None
     if s.kernels == "fused":
         kf = np.zeros(1)
@@ -354,12 +354,12 @@ def run_ours(args, rank, world):
         fused = {"bound": "hbm", "kernel": "k_step_fused (whole step, lossy, FP32%s)" % (", coded coefficients"
                                                                                          if coded else ""),
                  "achieved": ach_f, "peak": peak, "unit": "GB/s", "frac": ach_f / peak,
-                 "traffic": profile_traffic("fused_coded_cfg4_ncu.md" if coded else "fused_cfg4_ncu.md"),
+                 "traffic": profile_traffic("fused_coded_pillbox_ncu.md" if coded else "fused_pillbox_ncu.md"),
                  "algorithmic_bytes_per_launch": bytes_cell * N, "ms_per_launch": kf[0],
                  "peak_source": f"{src} HBM copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"}
         fused["traffic_source"] = ("profiles/%s: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
                                    "the 256x256x512 grid, scaled by the cell count (x8)"
-                                   % ("fused_coded_cfg4_ncu.md" if coded else "fused_cfg4_ncu.md"))
+                                   % ("fused_coded_pillbox_ncu.md" if coded else "fused_pillbox_ncu.md"))
         if coded:
             ach_model = BYTES_STEP_MODEL * N / (kf[0] / 1e3) / 1e9
             fused["coefficient_codes"] = s.coefficient_code_count
@@ -369,7 +369,7 @@ def run_ours(args, rank, world):
     out = {"metric": METRIC, "value": value, "unit": "Mcell-updates/s", "n_gpus": world, "steps": K, "warmup": W,
            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (analytic pillbox geometry, Gaussian beam)",
-           "config": {"workload": f"cfg4 pillbox {P.nx}x{P.ny}x{P.nz} FP32, sigma=5.8e7 walls (relaxation form), "
+           "config": {"workload": f"pillbox {P.nx}x{P.ny}x{P.nz} FP32, sigma=5.8e7 walls (relaxation form), "
                                   f"16-cell z PML, beam sigma_z=5 mm, 3x3 wake taps",
                       "cells": N, "run_steps": Nt, "cfln": P.cfln, "dt": float(s.dt),
                       "l2": "no flush: inputs (14 GB per step coded, 22 GB dense) far larger than the 129 MB L2",
@@ -386,7 +386,7 @@ def run_ours(args, rank, world):
            "gpu_launches": int(launches)}
     out["roofline"]["traffic_source"] = ("profiles/%s: ncu dram bytes of one launch on the 256x256x512 grid, "
                                          "scaled by the cell count (x8)"
-                                         % ("epass_coded_cfg4_ncu.md" if coded else "epass_cfg4_ncu.md"))
+                                         % ("epass_coded_pillbox_ncu.md" if coded else "epass_pillbox_ncu.md"))
     if fused is not None and coded and not args.no_dense_roofline:
         # the dense fused step on the same grid (84 B per cell-update: ch, ce, cl read per
         # cell), the step a grid with more than 65535 distinct coefficient triples runs
@@ -406,8 +406,8 @@ def run_ours(args, rank, world):
                                  "algorithmic_bytes_per_launch": BYTES_STEP_MODEL * N, "ms_per_launch": dense_ms[shape],
                                  "shape": {"vec": shape[0], "rows": shape[1], "zseg": shape[2], "ctas": shape[3]},
                                  "ms_by_shape": {"v%dr%dz%dc%d" % k: t for k, t in dense_ms.items()},
-                                 "traffic": profile_traffic("fused_cfg4_ncu.md"),
-                                 "traffic_source": "profiles/fused_cfg4_ncu.md (ncu, 256x256x512 grid, scaled x8)",
+                                 "traffic": profile_traffic("fused_pillbox_ncu.md"),
+                                 "traffic_source": "profiles/fused_pillbox_ncu.md (ncu, 256x256x512 grid, scaled x8)",
                                  "note": "the fused step of a grid whose coefficients do not compress (more than "
                                          "65535 distinct triples, e.g. graded spacing): 84 B per cell-update"}
     if fused is not None:
@@ -465,9 +465,9 @@ def serving_summary(args, peak):
 
     t_all = time.perf_counter()
     budget = int(args.serve_budget_gb * 1e9)
-    base = S.config3_requests(args.serve_count, seed=3)
+    base = S.cavity_sweep_requests(args.serve_count, seed=3)
     rate = S.poisson_rate_for(base, budget, args.serve_ref_rate * 1e9, load=args.serve_load)
-    reqs = S.config3_requests(args.serve_count, seed=3, rate_hz=rate)
+    reqs = S.cavity_sweep_requests(args.serve_count, seed=3, rate_hz=rate)
     out = {"workload": f"{len(reqs)} cavity wake solves (cube 20-60 mm, pipe 3-8 mm, n 48-160, z 2n, sigma_z 5-15 mm, "
                        f"PEC or sigma 1e3-1e6 S/m, wake 1 m), default_rng(seed=3)",
            "budget_bytes": budget, "arrival_rate_hz": rate, "chunk_steps": args.serve_chunk,
@@ -499,7 +499,7 @@ def serving_summary(args, peak):
     # every request resident: the pool's per-step throughput against the bytes its coded
     # two-pass kernels move (76 B per cell-update: E and H read and written once per pass
     # and a 2-byte code per pass) and against the 72 / 84 B per cell-update model
-    short = S.config3_requests(args.serve_count, seed=3, wakelength=0.1)
+    short = S.cavity_sweep_requests(args.serve_count, seed=3, wakelength=0.1)
     pool = nat.Pool(sum(S.footprint_bytes(r) for r in short) + (1 << 30), chunk_steps=args.serve_chunk)
     for vec, m in variants.items():
         pool.tune(vec, m)
@@ -577,8 +577,9 @@ def _rel(a, b, ref=None):
 
 def run_accuracy(args):
     """FP32 runs against the FP64 CUDA path (validated against the CPU oracle at 1e-10):
-    config 1 (both beam runs: fields, WP, WPx, WPy, Z, Zx, Zy), config 2 (64 probes of
-    Ez over 2000 steps) and, with --accuracy-cfg4, config 4 (WP over the first 0.3 m).
+    the lossy 128x128x256 cavity (both beam runs: fields, WP, WPx, WPy, Z, Zx, Zy), the
+    256^3 sphere (64 probes of Ez over 2000 steps) and, with --accuracy-pillbox, the
+    512x512x1024 pillbox (WP over the first 0.3 m).
 
     An FP32 solver rounds dt to float32, as the reference does.  The main comparison
     ("same_dt") runs FP64 at that rounded dt, so it isolates field precision.  The second
@@ -621,15 +622,15 @@ def run_accuracy(args):
                 "Zx": _rel(a["Zx"][:m], b["Zx"][:m], b["Z"][:m]), "Zy": _rel(a["Zy"][:m], b["Zy"][:m], b["Z"][:m]),
                 "E": _rel(a["E"], b["E"]), "H": _rel(a["H"], b["H"]), "Nt": [a["Nt"], b["Nt"]]}
 
-    for name in ("config1a", "config1b"):
-        case = CS.CONFIGS[name]
+    for name in ("lossy_cavity_128x128x256", "lossy_cavity_128x128x256_offset"):
+        case = CS.WORKLOADS[name]
         a = wake_run(case, np.float32)
         b = wake_run(case, np.float64, a["dt"])
         c = wake_run(case, np.float64)
         out[name] = {"same_dt": wake_err(a, b), "cfl_dt": wake_err(a, c), "dt_fp32": a["dt"], "dt_fp64": c["dt"],
                      "seconds_fp32": a["sec"], "seconds_fp64": b["sec"]}
-    # config 2: probes
-    case = CS.CONFIGS["config2"]
+    # the sphere and wave packet: probes
+    case = CS.WORKLOADS["sphere_packet_256"]
     P = CS.probe_points(case)
     probes = {}
     dt32 = None
@@ -649,11 +650,11 @@ def run_accuracy(args):
         del s, grid
         free()
     a, b = probes["fp32"][0], probes["fp64"][0]
-    out["config2"] = {"probe_Ez_rel_l2": _rel(a, b), "probe_Ez_max_abs_over_max": float(np.abs(a - b).max()
+    out["sphere_packet_256"] = {"probe_Ez_rel_l2": _rel(a, b), "probe_Ez_max_abs_over_max": float(np.abs(a - b).max()
                                                                                         / np.abs(b).max()),
                       "steps": case["Nt"], "probes": int(len(P)), "dt": "FP64 run at the FP32 run's dt",
                       "seconds_fp32": probes["fp32"][1], "seconds_fp64": probes["fp64"][1]}
-    if args.accuracy_cfg4:
+    if args.accuracy_pillbox:
         P4 = Pillbox()
         res = {}
         dt32 = None
@@ -669,7 +670,7 @@ def run_accuracy(args):
             del s, grid, wake
             free()
         a, b = res["fp32"], res["fp64"]
-        out["config4"] = {"WP_first_0.3m": _rel(a["WP"], b["WP"]), "Z": _rel(a["Z"], b["Z"]),
+        out["pillbox_512x512x1024"] = {"WP_first_0.3m": _rel(a["WP"], b["WP"]), "Z": _rel(a["Z"], b["Z"]),
                           "Nt": [a["Nt"], b["Nt"]], "dt": "FP64 run at the FP32 run's dt",
                           "seconds_fp32": a["sec"], "seconds_fp64": b["sec"]}
     print(json.dumps({"accuracy": out}), flush=True)
@@ -691,9 +692,9 @@ def run_serve(args):
     torch.cuda.set_device(dev)
     peak, src = peaks()
     budget = int(args.serve_budget_gb * 1e9)
-    base = S.config3_requests(args.serve_count, seed=3)
+    base = S.cavity_sweep_requests(args.serve_count, seed=3)
     rate = S.poisson_rate_for(base, budget, args.serve_ref_rate * 1e9, load=args.serve_load)
-    reqs = S.config3_requests(args.serve_count, seed=3, rate_hz=rate)
+    reqs = S.cavity_sweep_requests(args.serve_count, seed=3, rate_hz=rate)
     work_bytes = {r.tag: (84 if r.lossy else 72) for r in reqs}
 
     def model_bytes(recs):
@@ -809,7 +810,7 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
-def profile_traffic(name="epass_cfg4_ncu.md"):
+def profile_traffic(name="epass_pillbox_ncu.md"):
     """DRAM bytes per launch (scaled to the full grid) from a committed ncu summary."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
@@ -832,8 +833,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", type=int, nargs=3, default=None)
-    ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 errors on configs 1, 2 (and 4)")
-    ap.add_argument("--accuracy-cfg4", action="store_true")
+    ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 errors on the lossy cavity and the sphere (and the pillbox)")
+    ap.add_argument("--accuracy-pillbox", action="store_true")
     ap.add_argument("--serve", action="store_true", help="served wake solves: FP32 pool vs FP64 one at a time")
     ap.add_argument("--serve-count", type=int, default=64)
     ap.add_argument("--serve-budget-gb", type=float, default=4.0)
@@ -850,8 +851,9 @@ def main():
                     help="with --fused-shape: 0 loads, 1 or 2 TMA plane rings")
     ap.add_argument("--fused-shape", type=int, nargs=4, default=None, metavar=("VEC", "ROWS", "ZSEG", "CTAS"),
                     help="fused step tile shape (skips the autotuner)")
-    ap.add_argument("--cpu-configs", action="store_true",
-                    help="CPU oracle rates on configs 0-2 (FP64, FP32) and the config-0 time-to-impedance")
+    ap.add_argument("--cpu-workloads", action="store_true",
+                    help="CPU oracle rates on the cavity, lossy-cavity and sphere grids (FP64, FP32) and the "
+                         "60x60x120 cavity's time-to-impedance")
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--dense", action="store_true", help="fused step with dense coefficient arrays (no codes)")
     ap.add_argument("--variant", default="auto", choices=["auto", "staged", "direct", "fused"],
@@ -863,11 +865,11 @@ def main():
     if world > 1 and args.impl == "ours":
         import torch
         torch.distributed.init_process_group("nccl")
-    if args.cpu_configs:
-        run_cpu_configs(args)
+    if args.cpu_workloads:
+        run_cpu_workloads(args)
     elif args.serve:
         run_serve(args)
-    elif args.accuracy or args.accuracy_cfg4:
+    elif args.accuracy or args.accuracy_pillbox:
         run_accuracy(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)

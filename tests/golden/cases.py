@@ -93,7 +93,7 @@ def solids_for(c):
 _cavity_grid = dict(xmin=-30 * MM, xmax=30 * MM, ymin=-30 * MM, ymax=30 * MM, zmin=-60 * MM, zmax=60 * MM)
 
 CASES = {
-    # config-0 geometry at reduced size: PEC background, vacuum cube + pipe, ABC in z
+    # the 60x60x120 cavity geometry at reduced size: PEC background, vacuum cube + pipe, ABC in z
     "cavity_f64": dict(
         kind="wake", dtype="float64", grid=dict(_cavity_grid, Nx=16, Ny=16, Nz=32),
         solids=[("cavity", "cube_pipe", {}, [1.0, 1.0])], bg="pec",
@@ -110,7 +110,7 @@ CASES = {
         wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
                   fmax=5e9, skip_cells=2, counter_moving=True),
         wakelength=0.1, compute_plane="both"),
-    # config-1 physics at reduced size: sigma=1e4 walls (relaxation form), z PML, beta 0.8, offset 2 mm.
+    # the lossy 128x128x256 cavity physics at reduced size: sigma=1e4 walls (relaxation form), z PML, beta 0.8, offset 2 mm.
     # CFL 0.5 (the reference default): with sigma>0 cells the reference's explicit loss term
     # diverges at CFL 1.0 on this grid.
     "lossy_f64": dict(
@@ -168,7 +168,7 @@ CASES = {
         source=dict(type="PlaneWave", xs=(1, 11), ys=(1, 11), zs=1, beta=1.0, amplitude=1.0,
                     f_nodes=15, nodes=None, phase=0),
         Nt=90),
-    # config-2 layout at reduced size: PML on all faces, dielectric sphere, wave packet
+    # the 256^3 sphere layout at reduced size: PML on all faces, dielectric sphere, wave packet
     "wavepacket_f64": dict(
         kind="emsolve", dtype="float64",
         grid=dict(xmin=-1.0, xmax=1.0, ymin=-1.0, ymax=1.0, zmin=-1.0, zmax=1.0, Nx=16, Ny=16, Nz=16),
@@ -308,35 +308,35 @@ def refine_snaps(seed, xmin, xmax, nsnap):
 
 # ----------------------------------------------------------------------------- full configs
 # The benchmark workloads at full size (geometry analytic, evaluated at cell centres).
-CONFIGS = {
-    # config 0: plain FP64 PEC cubic cavity, 60x60x120, ABC in z, CFL 1.0, wake 0.5 m, fmax 5 GHz
-    "config0": dict(
+WORKLOADS = {
+    # plain FP64 PEC cubic cavity, 60x60x120, ABC in z, CFL 1.0, wake 0.5 m, fmax 5 GHz
+    "cavity_60x60x120": dict(
         kind="wake", dtype="float64", grid=dict(_cavity_grid, Nx=60, Ny=60, Nz=120),
         solids=[("cavity", "cube_pipe", {}, [1.0, 1.0])], bg="pec",
         bc_low=["pec", "pec", "abc"], bc_high=["pec", "pec", "abc"], cfln=1.0,
         wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
                   fmax=5e9, skip_cells=0),
         wakelength=0.5, compute_plane="both"),
-    # config 1, run a: 128x128x256, sigma = 1e4 walls (relaxation form), 10-cell z PML, beta 1
+    # lossy cavity, run a: 128x128x256, sigma = 1e4 walls (relaxation form), 10-cell z PML, beta 1
     # (CFL 0.5: the reference's explicit loss term diverges at CFL 1.0 with sigma > 0 cells)
-    "config1a": dict(
+    "lossy_cavity_128x128x256": dict(
         kind="wake", dtype="float32", grid=dict(_cavity_grid, Nx=128, Ny=128, Nz=256),
         solids=[("walls", "walls", {}, [1.0, 1.0, 1e4])], bg=[1.0, 1.0],
         bc_low=["pec", "pec", "pml"], bc_high=["pec", "pec", "pml"], n_pml=10, cfln=0.5,
         wake=dict(q=1e-9, sigmaz=10 * MM, beta=1.0, xsource=0.0, ysource=0.0, xtest=0.0, ytest=0.0,
                   fmax=5e9, skip_cells=0),
         wakelength=1.0, compute_plane="both"),
-    # config 1, run b: beta 0.8, source and test offset 2 mm in x
-    "config1b": dict(
+    # lossy cavity, run b: beta 0.8, source and test offset 2 mm in x
+    "lossy_cavity_128x128x256_offset": dict(
         kind="wake", dtype="float32", grid=dict(_cavity_grid, Nx=128, Ny=128, Nz=256),
         solids=[("walls", "walls", {}, [1.0, 1.0, 1e4])], bg=[1.0, 1.0],
         bc_low=["pec", "pec", "pml"], bc_high=["pec", "pec", "pml"], n_pml=10, cfln=0.5,
         wake=dict(q=1e-9, sigmaz=10 * MM, beta=0.8, xsource=2 * MM, ysource=0.0, xtest=2 * MM, ytest=0.0,
                   fmax=5e9, skip_cells=0),
         wakelength=1.0, compute_plane="both"),
-    # config 2: unit box [-1,1]^3 on 256^3, 12-cell PML on all faces, sphere r=0.25 eps_r=2,
+    # sphere and wave packet: unit box [-1,1]^3 on 256^3, 12-cell PML on all faces, sphere r=0.25 eps_r=2,
     # x-polarised wave packet along +z, centre wavelength 0.2, 2000 steps, 64 probes
-    "config2": dict(
+    "sphere_packet_256": dict(
         kind="emsolve", dtype="float32",
         grid=dict(xmin=-1.0, xmax=1.0, ymin=-1.0, ymax=1.0, zmin=-1.0, zmax=1.0, Nx=256, Ny=256, Nz=256),
         solids=[("sphere", "sphere", {"R": 0.25}, [2.0, 1.0])], bg=[1.0, 1.0],

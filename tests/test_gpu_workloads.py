@@ -1,10 +1,10 @@
 """Parity and accuracy at the benchmark workloads themselves (full size):
 
-* config 0 (FP64, 60x60x120, 1220 steps): the CUDA path against the CPU oracle within
+* the PEC cavity (FP64, 60x60x120, 1220 steps): the CUDA path against the CPU oracle within
   1e-10 relative L2 on WP, Z and the final fields;
 * the reference's own tests/test_001 golden vectors (FP32, 50x50x150, 5184 steps) with
   the tolerances of that test, and against the reference's full run of the same case;
-* config 1 (128x128x256 lossy, both beam runs): FP32 against the FP64 CUDA path (itself
+* the lossy cavity (128x128x256, both beam runs): FP32 against the FP64 CUDA path (itself
   checked against the oracle at 1e-10 on the smaller cases) -- WP within 1e-4.
 """
 
@@ -25,10 +25,10 @@ def _need_gpu():
         pytest.skip("needs a CUDA GPU")
 
 
-def test_config0_fp64_matches_oracle(tmp_path):
-    case = C.CONFIGS["config0"]
-    got = run_case("config0", case=case, tmpdir=tmp_path)
-    ref = run_oracle_case("config0", case=case)
+def test_cavity_60x60x120_fp64_matches_oracle(tmp_path):
+    case = C.WORKLOADS["cavity_60x60x120"]
+    got = run_case("cavity_60x60x120", case=case, tmpdir=tmp_path)
+    ref = run_oracle_case("cavity_60x60x120", case=case)
     assert int(got["Nt"]) == int(ref["Nt"])
     np.testing.assert_array_equal(got["s"], ref["s"])
     np.testing.assert_array_equal(got["f"], ref["f"])
@@ -67,14 +67,14 @@ def test_reference_test001_goldens_on_gpu(tmp_path):
     assert rel_l2(wake.Z, z["Z"]) < 1e-4
 
 
-@pytest.mark.parametrize("name", ["config1a", "config1b"])
-def test_config1_fp32_against_fp64(name, tmp_path):
+@pytest.mark.parametrize("name", ["lossy_cavity_128x128x256", "lossy_cavity_128x128x256_offset"])
+def test_lossy_cavity_fp32_against_fp64(name, tmp_path):
     """FP32 fields against FP64 fields at the same time step.  An FP32 solver rounds dt
     to float32 (as the reference does); run at the FP64 CFL step instead, the wake's time
     index int(.../dt) flips for some (s, z) pairs and moves WP near the bunch by ~1e-3
     -- a sampling effect of the post-processor, not of the field precision -- so the
     FP64 run is given the FP32 run's dt."""
-    case = C.CONFIGS[name]
+    case = C.WORKLOADS[name]
     r32 = run_case(name, case=case, tmpdir=tmp_path, dtype=np.float32)
     r64 = run_case(name, case=dict(case, dtype="float64"), tmpdir=tmp_path, dtype=np.float64, dt=float(r32["dt"]))
     assert int(r32["Nt"]) == int(r64["Nt"])
@@ -83,13 +83,13 @@ def test_config1_fp32_against_fp64(name, tmp_path):
     assert rel_l2(r32["Z"], r64["Z"]) < 1e-4
 
 
-def test_config1_coded_equals_dense(tmp_path, monkeypatch):
-    """The full config-1 run (128x128x256, lossy walls, PML, 4452 steps) with coded
+def test_lossy_cavity_coded_equals_dense(tmp_path, monkeypatch):
+    """The full lossy-cavity run (128x128x256, lossy walls, PML, 4452 steps) with coded
     coefficients gives the dense run's wake bit for bit."""
-    case = C.CONFIGS["config1a"]
+    case = C.WORKLOADS["lossy_cavity_128x128x256"]
     out = {}
     for codes in ("1", "0"):
         monkeypatch.setenv("WAKIS_GB300_CODES", codes)
-        out[codes] = run_case("config1a", case=case, tmpdir=tmp_path, dtype=np.float32)
+        out[codes] = run_case("lossy_cavity_128x128x256", case=case, tmpdir=tmp_path, dtype=np.float32)
     for k in ("WP", "Z", "WPx", "WPy", "E", "H"):
         np.testing.assert_array_equal(out["1"][k], out["0"][k], err_msg=k)

@@ -10,9 +10,9 @@ import wakis_gb300._native as nat
 from wakis_gb300 import serving as S
 
 
-def test_config3_requests_are_seeded_and_in_range():
-    a = S.config3_requests(64, seed=3)
-    b = S.config3_requests(64, seed=3)
+def test_cavity_sweep_requests_are_seeded_and_in_range():
+    a = S.cavity_sweep_requests(64, seed=3)
+    b = S.cavity_sweep_requests(64, seed=3)
     assert [dataclass_tuple(r) for r in a] == [dataclass_tuple(r) for r in b]
     assert len(a) == 64 and [r.tag for r in a] == list(range(64))
     for r in a:
@@ -24,7 +24,7 @@ def test_config3_requests_are_seeded_and_in_range():
         assert r.arrival == 0.0
         assert r.cells == 2 * r.n ** 3
     assert 10 < sum(r.lossy for r in a) < 54
-    c = S.config3_requests(64, seed=3, rate_hz=2.0)
+    c = S.cavity_sweep_requests(64, seed=3, rate_hz=2.0)
     t = np.array([r.arrival for r in c])
     assert np.all(np.diff(t) > 0)
     # same instances, only the arrival times are added
@@ -95,7 +95,7 @@ def test_admission_bypass_limit_protects_the_oldest_request():
 
 
 def test_poisson_rate_makes_the_queue_grow():
-    reqs = S.config3_requests(16, seed=3)
+    reqs = S.cavity_sweep_requests(16, seed=3)
     rate = S.poisson_rate_for(reqs, 4 << 30, service_rate_cells_per_s=50e9, load=1.5)
     work = np.mean([r.cells * S._steps_estimate(r) for r in reqs])
     assert rate == pytest.approx(1.5 * 50e9 / work)

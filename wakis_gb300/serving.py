@@ -35,8 +35,8 @@ MM = 1e-3
 
 @dataclasses.dataclass
 class CavityRequest:
-    """One wakefield solve of a cube cavity with a beam pipe (the cavity of config 0
-    scaled): vacuum = {|x|,|y|,|z| <= side/2} U {x^2 + y^2 <= rp^2}, domain
+    """One wakefield solve of a cube cavity with a beam pipe (the geometry of the 60x60x120
+    cavity wake run, scaled): vacuum = {|x|,|y|,|z| <= side/2} U {x^2 + y^2 <= rp^2}, domain
     x, y in [-0.6 side, 0.6 side], z in [-1.2 side, 1.2 side], n x n x 2n cells.
     sigma == 0: PEC walls (background PEC, ABC at the z ends, CFL 1.0).  sigma > 0: lossy
     walls [1, 1, sigma] (relaxation form), 10-cell PML at the z ends, CFL 0.5 (the
@@ -61,7 +61,7 @@ class CavityRequest:
         return self.sigma > 0
 
 
-def config3_requests(count=64, seed=3, rate_hz=None, wakelength=1.0):
+def cavity_sweep_requests(count=64, seed=3, rate_hz=None, wakelength=1.0):
     """The serving sweep's instances, drawn from numpy.random.default_rng(seed): cube side
     U(20, 60) mm, pipe radius U(3, 8) mm, cells per transverse dimension uniform in
     48..160 (z twice that), sigma_z U(5, 15) mm, walls PEC or lossy with sigma U(1e3, 1e6)
@@ -219,7 +219,7 @@ def run_resident(pool, reqs, kernels="direct"):
 
 
 def calibration_requests(seed=11, per_class=4, wakelength=0.1):
-    """Grids of the serving sweep's distribution (config3_requests' ranges) with Nx forced
+    """Grids of the serving sweep's distribution (cavity_sweep_requests' ranges) with Nx forced
     into each vector-width class: per class, per_class requests, half of them lossy."""
     rng = np.random.default_rng(seed)
     out = {}
