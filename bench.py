@@ -520,6 +520,9 @@ def serving_summary(args, peak):
                            "bytes": "hbm_frac on the 76 B per cell-update the coded two-pass kernels move; "
                                     "hbm_frac_model on the 72 B (PEC) / 84 B (lossy) model"}
     # plain FP64 one at a time on a subsample: solves/h and the FP32 results' errors
+    if args.serve_fp64_sample <= 0:
+        out["seconds"] = time.perf_counter() - t_all
+        return out
     rng = np.random.default_rng(5)
     sub = sorted(rng.choice(len(reqs), size=min(args.serve_fp64_sample, len(reqs)), replace=False).tolist())
     res64 = {}
