@@ -48,6 +48,16 @@ def test_ctx_create_rejects_bad_arguments_without_gpu():
     if not torch.cuda.is_available():
         d.dtype = 0
         assert lib.fit_ctx_create(ctypes.byref(d), ctypes.byref(h)) == -6  # no device
+    # cells are addressed by 32-bit offsets within a component: N + Nx*Ny < 2^31
+    d.dtype = 0
+    d.nx, d.ny, d.nz = 1290, 1290, 1290  # N = 2146689000 < 2^31, N + Nx*Ny above it: refused
+    assert lib.fit_ctx_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    assert "too large" in nat.last_error(None)
+    d.nx, d.ny, d.nz = 32768, 32768, 2  # N = 2^31: refused
+    assert lib.fit_ctx_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    d.nx, d.ny, d.nz = 16384, 16384, 7  # N + Nx*Ny = 2^31 exactly: refused
+    assert lib.fit_ctx_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    assert "too large" in nat.last_error(None)
 
 
 def test_bc_codes():
