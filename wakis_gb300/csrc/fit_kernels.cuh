@@ -1017,10 +1017,12 @@ __global__ void __launch_bounds__(256, 4) k_epass_pair(T* __restrict__ E, const 
 // ce and cl read once); halo reads of the neighbouring tiles hit L2.
 // planes ahead whose first-touch data (E of plane k+PF+1 along x and y, E_z, H and the
 // codes of plane k+PF) a row warp of the coded step asks L2 to fetch while it works on
-// plane k; 0: off.  On the 512x512x1024 pillbox (4 rows) distances 0, 1, 2, 3 ran 2.89,
-// 2.62, 2.58 and 2.70 ms per step; the same prefetch for the halo row gained nothing.
+// plane k; 0: off.  On the 512x512x1024 pillbox (4 rows) distances 0, 1, 2, 3 first ran
+// 2.89, 2.62, 2.58 and 2.70 ms per step; with the explicitly rounded arithmetic and 32-bit
+// offsets, 1, 2, 3 run 2.654, 2.677 and 2.706 ms (autotuned shapes).  The same prefetch
+// for the halo row gained nothing.
 #ifndef FIT_FUSED_PREFETCH
-#define FIT_FUSED_PREFETCH 2
+#define FIT_FUSED_PREFETCH 1
 #endif
 
 
